@@ -1,0 +1,260 @@
+/*
+ * mtr.h - C ABI of libmtr, a single-GPU (GB300, sm_103a) multi-axis
+ * tomographic reconstruction library: weighted back-projection init, SIRT
+ * with bilinear forward/back projectors, and MACE consensus over tilt axes.
+ *
+ * Plain C types only: pointers, sizes, status codes.  Every entry point
+ * returns an mtr_status; nothing here prints or exits.  A context is bound
+ * to one CUDA device and one stream and is not thread-safe (use one context
+ * per host thread).
+ *
+ * Each entry point names the interface of the reference program
+ * (Autumn1998/Multi-tilt-Reconstuction) that it replaces, as file:line.
+ */
+#ifndef MTR_H_
+#define MTR_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MTR_ABI_VERSION 1
+/* Maximum tilt axes per reconstruction (MAX_TILT, ReadAndInitialOptions.h:17). */
+#define MTR_MAX_AXES 16
+/* Default SIRT iterations per MACE iteration (hard-coded, FunctionOnGPU.cu:212). */
+#define MTR_DEFAULT_SIRT_INNER 10
+
+typedef enum mtr_status {
+  MTR_OK = 0,
+  MTR_ERR_INVALID_ARGUMENT = 1,
+  MTR_ERR_CUDA = 2,
+  MTR_ERR_OUT_OF_MEMORY = 3,
+  MTR_ERR_IO = 4,
+  MTR_ERR_FORMAT = 5,
+  MTR_ERR_UNSUPPORTED = 6,
+  MTR_ERR_NO_DEVICE = 7,
+  MTR_ERR_TIMEOUT = 8,
+  MTR_ERR_NOT_READY = 9,
+  MTR_ERR_CAPACITY = 10
+} mtr_status;
+
+/* Storage precision.  FP32: everything float.  MIXED_*: projections and
+ * residuals stored FP16, the volume copy read by the forward projector
+ * stored BF16 (or FP16); interpolation and accumulation in FP32; residual
+ * norms and the MACE consensus sum in FP64; the SIRT iterate and the MACE
+ * state stay FP32. */
+typedef enum mtr_precision {
+  MTR_PREC_FP32 = 0,
+  MTR_PREC_MIXED_BF16 = 1,
+  MTR_PREC_MIXED_FP16 = 2
+} mtr_precision;
+
+/* Where a buffer passed to an entry point lives. */
+typedef enum mtr_mem_kind { MTR_MEM_HOST = 0, MTR_MEM_DEVICE = 1 } mtr_mem_kind;
+
+/* Volume frame, absolute voxel coordinates, end-exclusive, X = Xend-Xstart.
+ * Same fields and order as VolumeSize (MrcFileIOBaseFunction.h:57-70). */
+typedef struct mtr_volume_size {
+  int Xstart, Xend, Ystart, Yend, Zstart, Zend;
+  int X, Y, Z;
+} mtr_volume_size;
+
+/* Detector size and angle count.  Same fields as ProjectionSize
+ * (MrcFileIOBaseFunction.h:73-78). */
+typedef struct mtr_projection_size {
+  int X, Y, AngN;
+} mtr_projection_size;
+
+/* One tilt axis: projections [AngN][Y][X] (x fastest) and per-angle affine
+ * maps, 4 doubles per angle [const, X, Y, Z], detector coordinate
+ * = c0 + c1*X + c2*Y + c3*Z - 1 (FunctionOnGPU.cu:12-25). */
+typedef struct mtr_axis {
+  mtr_projection_size prj;
+  const double* x_coef; /* 4*AngN, host memory */
+  const double* y_coef; /* 4*AngN, host memory */
+  const float* prj_data; /* AngN*Y*X floats; host or device (see mem_kind) */
+} mtr_axis;
+
+typedef struct mtr_params {
+  int iter_times;   /* -n: MACE outer iterations (ReadAndInitialOptions.h:38, default 5) */
+  int sirt_inner;   /* SIRT iterations per MACE iteration (default 10) */
+  float sirt_step;  /* -s: SIRT relaxation (default 0.5) */
+  float mace_step;  /* -m: MACE Mann step rho (default 0.7) */
+  int precision;    /* mtr_precision */
+  int flags;        /* MTR_FLAG_* */
+} mtr_params;
+
+/* Record the squared residual norm (FP64) of every SIRT iteration. */
+#define MTR_FLAG_RECORD_NORMS 1
+/* Capture the MACE outer iteration in a CUDA graph and replay it. */
+#define MTR_FLAG_GRAPH 2
+
+/* Fill p with the reference defaults (Options(), ReadAndInitialOptions.h:33-42). */
+void mtr_params_default(mtr_params* p);
+
+typedef struct mtr_context mtr_context;
+
+/* Library / error information. */
+int mtr_abi_version(void);
+const char* mtr_status_string(mtr_status s);
+const char* mtr_context_last_error(const mtr_context* ctx);
+
+/* Context: device, stream, scratch.  device < 0 selects the current device.
+ * Replaces the per-call cudaSetDevice(rank%4)/cudaStreamCreate of the
+ * reference entry points (FunctionOnGPU.cu:140,150-151,184,193-194). */
+mtr_status mtr_context_create(int device, mtr_context** out);
+mtr_status mtr_context_destroy(mtr_context* ctx);
+/* Use an external cudaStream_t (NULL restores the context's own stream). */
+mtr_status mtr_context_set_stream(mtr_context* ctx, void* cuda_stream);
+mtr_status mtr_context_synchronize(mtr_context* ctx);
+/* Number of libmtr kernel launches issued by this context so far. */
+mtr_status mtr_context_launch_count(const mtr_context* ctx, long long* out);
+
+/* ---- Entry points replacing FunctionOnGPU.cuh:41-44 -------------------- */
+
+/* Replaces ComputeInitialModel (FunctionOnGPU.cuh:41, FunctionOnGPU.cu:138-179).
+ * Weighted back-projection of one axis over the Z-slab [slice_start,
+ * slice_end) of vol: slab_out[(x)+(y)*X+(z-slice_start)*X*Y] = s/c where the
+ * in-detector bilinear weight sum c != 0, else 0 (the reference adds into a
+ * fresh device buffer; it is treated as zero).  slab_out is host memory. */
+mtr_status mtr_wbp(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol, int slice_start,
+                   int slice_end, float* slab_out);
+
+/* Replaces runSIRTOnGPU (FunctionOnGPU.cuh:42, FunctionOnGPU.cu:182-266) for
+ * a caller that holds the whole Z range of its axis (no MPI communicator):
+ * n_inner SIRT iterations x <- x + sirt_step * C A^T (b - R A x) on the
+ * host slab, in place.  The reference hard-codes n_inner = 10. */
+mtr_status mtr_sirt(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol, int slice_start,
+                    int slice_end, int n_inner, float sirt_step, float* slab_inout);
+
+/* Replaces initialZdata (FunctionOnGPU.cuh:43, FunctionOnGPU.cu:291-313):
+ * z = 2*w_avg - w over the whole volume (host buffers). */
+mtr_status mtr_initial_z(mtr_context* ctx, mtr_volume_size vol, const float* w, const float* w_avg,
+                         float* z);
+
+/* Replaces runMaceOnGPU (FunctionOnGPU.cuh:44, FunctionOnGPU.cu:336-362) and
+ * runMaceOnCPU (MultiAxis.cpp:33-38): w = step*(2v - z) + (1-step)*w. */
+mtr_status mtr_update_w(mtr_context* ctx, mtr_volume_size vol, const float* v, const float* z, float* w,
+                        float step);
+
+/* Replaces the whole of MultiAxis.cpp:101-230 after option and file parsing:
+ * per-axis WBP summed into the initial model (MultiAxis.cpp:172-200), then
+ * iter_times MACE iterations of sirt_inner SIRT iterations per axis with the
+ * consensus mean (MultiAxis.cpp:40-71), on one GPU.  out_volume receives
+ * w_avg (X*Y*Z floats, x fastest), host memory. */
+mtr_status mtr_reconstruct(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
+                           const mtr_params* params, float* out_volume);
+
+/* ---- Device-resident reconstruction object ------------------------------ */
+/* The same computation as mtr_reconstruct, split so that uploads, the
+ * on-device run and the download can be issued (and timed) separately. */
+typedef struct mtr_recon mtr_recon;
+
+/* axes[i].prj_data is host memory (mem_kind MTR_MEM_HOST) or device memory
+ * (MTR_MEM_DEVICE, float, copied device-to-device). */
+mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
+                            const mtr_params* params, int mem_kind, mtr_recon** out);
+/* Re-upload projection data for axis i (same shape). */
+mtr_status mtr_recon_upload(mtr_recon* r, int axis, const float* prj_data, int mem_kind);
+/* WBP init + MACE loop on the device (asynchronous on the context stream). */
+mtr_status mtr_recon_run(mtr_recon* r);
+/* Copy w_avg out (host or device destination); synchronises for host. */
+mtr_status mtr_recon_download(mtr_recon* r, float* out, int mem_kind);
+/* Copy the K per-axis MACE states w_k (K*X*Y*Z floats). */
+mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind);
+/* Squared residual norms, n_outer*K*n_inner doubles (MTR_FLAG_RECORD_NORMS). */
+mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n);
+/* Device bytes held by the object. */
+mtr_status mtr_recon_footprint(const mtr_recon* r, long long* bytes);
+mtr_status mtr_recon_destroy(mtr_recon* r);
+/* Device bytes an object with these shapes would hold (admission control). */
+mtr_status mtr_estimate_footprint(int n_axes, const mtr_projection_size* prjs, mtr_volume_size vol,
+                                  int precision, long long* bytes);
+
+/* ---- MRC / TXBR / options (the reference's file I/O boundary) ----------- */
+
+/* 1024-byte MRC header, same layout as MrcHeader (MrcFileIOBaseFunction.h:99-173). */
+#pragma pack(push, 1)
+typedef struct mtr_mrc_header {
+  int nx, ny, nz, mode;
+  int nxstart, nystart, nzstart;
+  int mx, my, mz;
+  float xlen, ylen, zlen;
+  float alpha, beta, gamma;
+  int mapc, mapr, maps;
+  float amin, amax, amean;
+  short ispg, nsymbt;
+  int next;
+  short creatid;
+  char blank[30];
+  short nint, nreal;
+  short sub, zfac;
+  float min2, max2, min3, max3, min4, max4;
+  short idtype, lens, nd1, nd2, vd1, vd2;
+  float tiltangles[6];
+  float xorg, yorg, zorg;
+  char cmap[4];
+  char stamp[4];
+  float rms;
+  int nlabl;
+  char labels[10][80];
+} mtr_mrc_header;
+#pragma pack(pop)
+
+#define MTR_MRC_MODE_BYTE 0
+#define MTR_MRC_MODE_SHORT 1
+#define MTR_MRC_MODE_FLOAT 2
+#define MTR_MRC_MODE_USHORT 6
+#define MTR_MRC_MODE_HALF 12
+
+/* Replaces mrcReadhead (MrcFileIOBaseFunction.cpp:11-16). */
+mtr_status mtr_mrc_read_header(const char* path, mtr_mrc_header* out);
+/* Replaces mrcReadAllData (MrcFileIOBaseFunction.cpp:18-70): n = nx*ny*nz
+ * values converted to float.  The data block is the LAST n*bytes(mode)
+ * bytes of the file (the reference takes file_size - n*2 for every mode,
+ * which is the same offset for 16-bit modes).  Modes 0,1,2,6,12. */
+mtr_status mtr_mrc_read_stack(const char* path, float* out, long long n);
+/* Replaces readCoef (MrcFileIOBaseFunction.cpp:72-134).  Appends x/y
+ * coefficients (up to cap each), counts them in *n_x / *n_y, widens *vol by
+ * the x->, y->, z-> bound lines and sets vol->X/Y/Z = end - start. */
+mtr_status mtr_txbr_read(const char* path, double* x_coef, double* y_coef, int cap, int* n_x, int* n_y,
+                         mtr_volume_size* vol);
+/* Initialise a volume frame to the reference's empty bounds
+ * (Xstart=999999, Xend=-999999, ..., MrcFileIO.h:22-28). */
+void mtr_volume_size_empty(mtr_volume_size* vol);
+/* Replaces updataAndWriteModel/writeModel (MrcFileIO.cpp:180-201): float32
+ * MRC with the reference's header fields (MrcFileIO.cpp:3-61) and amin /
+ * amax / amean computed from data (amean = mean of per-section means). */
+mtr_status mtr_mrc_write_volume(const char* path, mtr_volume_size vol, const float* data);
+/* Write a projection stack [nz][ny][nx] (modes 1, 2 or 12) with a minimal
+ * header; used to produce test inputs in the reference's format. */
+mtr_status mtr_mrc_write_stack(const char* path, int nx, int ny, int nz, int mode, const float* data);
+
+/* Parsed command line (readOptions, ReadAndInitialOptions.cpp:127-172). */
+typedef struct mtr_options {
+  int number_tilt;
+  char mrc_path[MTR_MAX_AXES][1024];
+  char txbr_path[MTR_MAX_AXES][1024];
+  char out_path[1024];
+  int block_x, block_y, block_z; /* -x -y -z, kept as tile hints */
+  int iter_times;                /* -n */
+  float sirt_step;               /* -s */
+  float mace_step;               /* -m */
+  int sirt_inner;                /* --inner (long option; default 10) */
+  int precision;                 /* --precision fp32|bf16|fp16 */
+  int help;                      /* -h given */
+} mtr_options;
+
+/* Same short options as the reference (-h -i -o -x -y -z -n -s -m) plus the
+ * long options --inner N and --precision P.  Unlike the reference, an
+ * invalid option or a malformed -i list is an error (MTR_ERR_INVALID_ARGUMENT). */
+mtr_status mtr_parse_options(int argc, char** argv, mtr_options* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MTR_H_ */

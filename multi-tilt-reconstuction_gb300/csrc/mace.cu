@@ -1,0 +1,147 @@
+// Elementwise and MACE consensus kernels (sm_103a).  These are HBM-bound:
+// grid-stride loops over the volume, sized to a multiple of the SM count.
+#include "mtr_internal.h"
+
+namespace mtr {
+namespace {
+
+constexpr int kThreads = 256;
+
+unsigned grid_for(long long n) {
+  long long b = (n + kThreads - 1) / kThreads;
+  const long long cap = 152LL * 8;  // 8 resident CTAs per SM on 152 SMs
+  if (b > cap) b = cap;
+  if (b < 1) b = 1;
+  return (unsigned)b;
+}
+
+__global__ void fill_kernel(float* __restrict__ p, long long n, float v) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+__global__ void add_kernel(float* __restrict__ dst, const float* __restrict__ src, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = __fadd_rn(dst[i], src[i]);
+}
+
+// z = 2*w_avg - w (FunctionOnGPU.cu:268-276).
+__global__ void initial_z_kernel(const float* __restrict__ w, const float* __restrict__ wavg, float* __restrict__ z,
+                                 long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[i] = __fsub_rn(2.f * wavg[i], w[i]);
+}
+
+// w = step*(2v - z) + (1-step)*w, with the reference host loop's float
+// rounding (MultiAxis.cpp:33-38; no fused multiply-add).
+__device__ __forceinline__ float mann(float v, float z, float w, float step) {
+  const float t1 = __fsub_rn(2.f * v, z);
+  const float t2 = __fmul_rn(step, t1);
+  const float t3 = __fmul_rn(__fsub_rn(1.f, step), w);
+  return __fadd_rn(t2, t3);
+}
+
+__global__ void update_w_kernel(const float* __restrict__ v, const float* __restrict__ z, float* __restrict__ w,
+                                long long n, float step) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    w[i] = mann(v[i], z[i], w[i], step);
+}
+
+__global__ void convert_kernel(const float* __restrict__ src, void* __restrict__ dst, int kind, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (kind == 1) static_cast<__nv_bfloat16*>(dst)[i] = __float2bfloat16_rn(src[i]);
+    else static_cast<__half*>(dst)[i] = __float2half_rn(src[i]);
+  }
+}
+
+// One MACE outer step for all K axes at once, replacing the reference's
+// initialZdata + runMaceOnCPU + Reduce/Bcast consensus (FunctionOnGPU.cu:268-313,
+// MultiAxis.cpp:48-67).  On entry x[k] holds v_k = SIRT(z_k), w[k] the state
+// w_k and wavg the consensus that z_k was formed from (z_k = 2 wavg - w_k,
+// recomputed here instead of stored).  On exit:
+//   w[k] = rho*(2 v_k - z_k) + (1-rho) w_k
+//   wavg = (sum_k w[k]) / K      (summed in FP64)
+//   x[k] = 2 wavg - w[k]         (the next outer iteration's z_k)
+// and, when copy_kind != 0, x_copy[k] = x[k] in bf16/f16 for the forward pass.
+// dchange (optional) accumulates sum (wavg_new - wavg_old)^2 in FP64.
+constexpr int kMaxK = MTR_MAX_AXES;
+struct MacePtrs {
+  float* w[kMaxK];
+  float* x[kMaxK];
+  void* xc[kMaxK];
+};
+
+__global__ void __launch_bounds__(kThreads)
+mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho, int copy_kind,
+            double* __restrict__ dchange) {
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float wa = wavg[i];
+    float wn[kMaxK];
+    double sum = 0.0;
+#pragma unroll
+    for (int k = 0; k < kMaxK; ++k) {
+      if (k < K) {
+        const float wk = P.w[k][i];
+        const float zk = __fsub_rn(2.f * wa, wk);
+        wn[k] = mann(P.x[k][i], zk, wk, rho);
+        P.w[k][i] = wn[k];
+        sum += (double)wn[k];
+      }
+    }
+    const float na = (float)(sum / (double)K);
+    wavg[i] = na;
+    const double d = (double)na - (double)wa;
+    acc += d * d;
+#pragma unroll
+    for (int k = 0; k < kMaxK; ++k) {
+      if (k < K) {
+        const float zn = __fsub_rn(2.f * na, wn[k]);
+        P.x[k][i] = zn;
+        if (copy_kind == 1) static_cast<__nv_bfloat16*>(P.xc[k])[i] = __float2bfloat16_rn(zn);
+        else if (copy_kind == 2) static_cast<__half*>(P.xc[k])[i] = __float2half_rn(zn);
+      }
+    }
+  }
+  if (dchange) {
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ double red[kThreads / 32];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+      atomicAdd(dchange, t);
+    }
+  }
+}
+
+}  // namespace
+
+void launch_fill(float* p, long long n, float v, cudaStream_t st) {
+  fill_kernel<<<grid_for(n), kThreads, 0, st>>>(p, n, v);
+}
+void launch_axpy_acc(float* dst, const float* src, long long n, cudaStream_t st) {
+  add_kernel<<<grid_for(n), kThreads, 0, st>>>(dst, src, n);
+}
+void launch_initial_z(const float* w, const float* wavg, float* z, long long n, cudaStream_t st) {
+  initial_z_kernel<<<grid_for(n), kThreads, 0, st>>>(w, wavg, z, n);
+}
+void launch_update_w(const float* v, const float* z, float* w, long long n, float step, cudaStream_t st) {
+  update_w_kernel<<<grid_for(n), kThreads, 0, st>>>(v, z, w, n, step);
+}
+void launch_convert_copy(const float* src, void* dst, int copy_kind, long long n, cudaStream_t st) {
+  convert_kernel<<<grid_for(n), kThreads, 0, st>>>(src, dst, copy_kind, n);
+}
+void launch_mace(int K, float* const* w, float* const* x, float* wavg, long long n, float rho, void* const* x_copy,
+                 int copy_kind, double* dchange, cudaStream_t st) {
+  MacePtrs P{};
+  for (int k = 0; k < K && k < kMaxK; ++k) {
+    P.w[k] = w[k];
+    P.x[k] = x[k];
+    P.xc[k] = x_copy ? x_copy[k] : nullptr;
+  }
+  mace_kernel<<<grid_for(n), kThreads, 0, st>>>(K, P, wavg, n, rho, copy_kind, dchange);
+}
+
+}  // namespace mtr

@@ -1,0 +1,118 @@
+// Host runtime pieces shared by the C ABI translation units: the context,
+// device buffers, error plumbing and the device-resident reconstruction.
+#pragma once
+
+#include <atomic>
+#include <string>
+#include <vector>
+
+#include "mtr_internal.h"
+
+struct mtr_context {
+  int device = 0;
+  int num_sms = 152;
+  int cc_major = 0, cc_minor = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+};
+
+namespace mtr {
+
+// Process-wide count of libmtr kernel launches (graph replays add their node count).
+extern std::atomic<long long> g_launches;
+
+mtr_status set_error(mtr_context* ctx, mtr_status s, const std::string& msg);
+mtr_status cuda_error(mtr_context* ctx, cudaError_t e, const char* what);
+mtr_status check_volume(mtr_context* ctx, const mtr_volume_size& v);
+mtr_status check_axis(mtr_context* ctx, const mtr_axis& a);
+
+// Makes a device current for a scope and restores the previous one.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+// Owning device allocation.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf& operator=(DevBuf&& o) noexcept {
+    if (this != &o) { reset(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    return *this;
+  }
+  ~DevBuf() { reset(); }
+  cudaError_t alloc(size_t n) {
+    reset();
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n; else p = nullptr;
+    return e;
+  }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  template <typename T> T* as() const { return static_cast<T*>(p); }
+};
+
+#define MTR_CK(ctx, call)                                       \
+  do {                                                          \
+    cudaError_t _e = (call);                                    \
+    if (_e != cudaSuccess) return ::mtr::cuda_error((ctx), _e, #call); \
+  } while (0)
+
+#define MTR_CK_LAUNCH(ctx, what)                                \
+  do {                                                          \
+    ::mtr::g_launches.fetch_add(1, std::memory_order_relaxed);  \
+    cudaError_t _e = cudaGetLastError();                        \
+    if (_e != cudaSuccess) return ::mtr::cuda_error((ctx), _e, what); \
+  } while (0)
+
+// Per-axis device state of a reconstruction.
+struct AxisState {
+  int PX = 0, PY = 0, A = 0;
+  long long np = 0;       // A*PY*PX
+  DevBuf xc, yc;          // [A*4] doubles
+  DevBuf b;               // projections: float (FP32) or half (mixed)
+  DevBuf s;               // forward accumulator, float
+  DevBuf cf;              // forward row sums A 1, float
+  DevBuf r;               // residual: float or half
+  DevBuf cbp;             // back-projection weight sums A^T 1 (volume), float
+  DevBuf w;               // MACE state w_k (volume), float
+  DevBuf x;               // SIRT iterate z_k -> v_k (volume), float
+  DevBuf xcopy;           // bf16/f16 copy of x read by the forward pass (mixed)
+  AxisDev dev() const { return AxisDev{PX, PY, A, xc.as<double>(), yc.as<double>()}; }
+};
+
+}  // namespace mtr
+
+struct mtr_recon {
+  mtr_context* ctx = nullptr;
+  mtr_volume_size vs{};
+  mtr::VolDev vol{};
+  mtr_params p{};
+  int K = 0;
+  long long nv = 0;
+  std::vector<mtr::AxisState> ax;
+  mtr::DevBuf wavg;       // consensus volume, float
+  mtr::DevBuf norms;      // n_outer*K*n_inner doubles
+  mtr::DevBuf dchange;    // n_outer doubles
+  long long bytes = 0;
+  bool geometry_ready = false;  // cf and cbp computed
+  cudaGraphExec_t graph = nullptr;
+  long long graph_nodes = 0;
+  ~mtr_recon();
+};

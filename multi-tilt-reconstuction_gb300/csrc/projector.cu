@@ -1,0 +1,283 @@
+// Bilinear projector kernels for the multi-axis SIRT path (sm_103a).
+//
+// Geometry (the reference's computeWeight, FunctionOnGPU.cu:12-25): voxel
+// (X,Y,Z) lands on detector coordinate
+//     x = a0 + a1 X + a2 Y + a3 Z - 1,   y = b0 + b1 X + b2 Y + b3 Z - 1
+// and touches the four pixels (ix,iy), (ix+1,iy), (ix,iy+1), (ix+1,iy+1),
+// ix = floor(x), with bilinear weights (1-dx)(1-dy), dx(1-dy), (1-dx)dy,
+// dx dy.  Taps outside the detector are dropped (FunctionOnGPU.cu:27-79).
+//
+// Coordinates: the reference evaluates the map in FP64 per voxel and angle.
+// Here each CTA evaluates it once per angle in FP64 at its base voxel, splits
+// the result into an integer part and a float fraction in [0,1), and each
+// thread adds float slope * (small offset) to the fraction.  The float part
+// stays below ~100 in magnitude, so the tap position carries ~1e-5 px of
+// error however large the detector is, and the inner loop is pure FP32.
+#include "mtr_internal.h"
+
+namespace mtr {
+namespace {
+
+// Split-precision affine map of one angle relative to a CTA base voxel.
+struct AngleConst {
+  float xf, a1, a2, a3;
+  float yf, b1, b2, b3;
+  int xi, yi;
+};
+
+__device__ __forceinline__ int clamp_int_base(double v) {
+  // Keep the integer base far from int overflow when it is added to small
+  // offsets; anything this far off the detector is dropped by the tap tests.
+  v = fmin(fmax(v, -1.0e9), 1.0e9);
+  return (int)v;
+}
+
+__device__ __forceinline__ void make_angle_const(const double* __restrict__ xc, const double* __restrict__ yc,
+                                                 int a, int X0, int Y0, int Z0, AngleConst& k) {
+  const double* cx = xc + 4 * a;
+  const double* cy = yc + 4 * a;
+  const double xb = cx[0] + cx[1] * X0 + cx[2] * Y0 + cx[3] * Z0 - 1.0;
+  const double yb = cy[0] + cy[1] * X0 + cy[2] * Y0 + cy[3] * Z0 - 1.0;
+  const double fxb = floor(xb), fyb = floor(yb);
+  k.xi = clamp_int_base(fxb);
+  k.yi = clamp_int_base(fyb);
+  k.xf = (float)(xb - fxb);
+  k.yf = (float)(yb - fyb);
+  k.a1 = (float)cx[1]; k.a2 = (float)cx[2]; k.a3 = (float)cx[3];
+  k.b1 = (float)cy[1]; k.b2 = (float)cy[2]; k.b3 = (float)cy[3];
+}
+
+template <typename T> __device__ __forceinline__ float ld_f(const T* p);
+template <> __device__ __forceinline__ float ld_f<float>(const float* p) { return __ldg(p); }
+template <> __device__ __forceinline__ float ld_f<__half>(const __half* p) { return __half2float(__ldg(p)); }
+template <> __device__ __forceinline__ float ld_f<__nv_bfloat16>(const __nv_bfloat16* p) {
+  return __bfloat162float(__ldg(p));
+}
+
+template <typename T> __device__ __forceinline__ T from_f(float v);
+template <> __device__ __forceinline__ float from_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ __half from_f<__half>(float v) { return __float2half_rn(v); }
+template <> __device__ __forceinline__ __nv_bfloat16 from_f<__nv_bfloat16>(float v) { return __float2bfloat16_rn(v); }
+
+constexpr int kTX = 32;  // CTA tile in X (one warp row)
+constexpr int kTY = 8;   // CTA tile in Y
+constexpr int kZR = 8;   // voxels per thread along Z
+
+// Back-projection gather over all angles.
+//   MODE 0 (WBP, FunctionOnGPU.cu:82-109): vol_out = s/c (0 where c == 0), cbp = c.
+//   MODE 1 (SIRT, FunctionOnGPU.cu:111-135): vol_out += step * s/cbp where cbp != 0.
+//   MODE 2: cbp = c only.
+// copy_kind 1/2 additionally writes the updated voxel as bf16/f16 to vol_copy.
+template <typename PT, int MODE>
+__global__ void __launch_bounds__(kTX * kTY)
+bp_gather_kernel(AxisDev ax, VolDev vol, const PT* __restrict__ img, float step, float* __restrict__ vol_out,
+                 float* __restrict__ cbp, void* __restrict__ vol_copy, int copy_kind, int z0, int z1) {
+  extern __shared__ AngleConst sk[];
+  const int tid = threadIdx.x + threadIdx.y * kTX;
+  const int X0 = vol.Xs + blockIdx.x * kTX;
+  const int Y0 = vol.Ys + blockIdx.y * kTY;
+  const int Z0 = z0 + blockIdx.z * kZR;
+  for (int a = tid; a < ax.A; a += kTX * kTY) make_angle_const(ax.xc, ax.yc, a, X0, Y0, Z0, sk[a]);
+  __syncthreads();
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  if (X0 + tx >= vol.Xs + vol.NX || Y0 + ty >= vol.Ys + vol.NY) return;
+  const int PX = ax.PX, PY = ax.PY;
+  const long long plane = (long long)PX * PY;
+
+  float s[kZR], c[kZR];
+#pragma unroll
+  for (int z = 0; z < kZR; ++z) { s[z] = 0.f; c[z] = 0.f; }
+
+  for (int a = 0; a < ax.A; ++a) {
+    const AngleConst k = sk[a];
+    const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
+    const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
+    const PT* im = img + plane * a;
+#pragma unroll
+    for (int z = 0; z < kZR; ++z) {
+      const float x = fmaf(k.a3, (float)z, xr);
+      const float y = fmaf(k.b3, (float)z, yr);
+      const float flx = floorf(x), fly = floorf(y);
+      const float fx = x - flx, fy = y - fly;
+      const int ix = k.xi + (int)flx, iy = k.yi + (int)fly;
+      const bool x0 = (unsigned)ix < (unsigned)PX, x1 = (unsigned)(ix + 1) < (unsigned)PX;
+      const bool y0 = (unsigned)iy < (unsigned)PY, y1 = (unsigned)(iy + 1) < (unsigned)PY;
+      if (MODE != 2) {
+        const PT* row0 = im + (long long)iy * PX + ix;
+        const PT* row1 = row0 + PX;
+        const float p00 = (x0 && y0) ? ld_f(row0) : 0.f;
+        const float p10 = (x1 && y0) ? ld_f(row0 + 1) : 0.f;
+        const float p01 = (x0 && y1) ? ld_f(row1) : 0.f;
+        const float p11 = (x1 && y1) ? ld_f(row1 + 1) : 0.f;
+        const float r0 = fmaf(fx, p10 - p00, p00);
+        const float r1 = fmaf(fx, p11 - p01, p01);
+        s[z] += fmaf(fy, r1 - r0, r0);
+      }
+      if (MODE != 1) {
+        const float cx = (x0 ? 1.f - fx : 0.f) + (x1 ? fx : 0.f);
+        const float cy = (y0 ? 1.f - fy : 0.f) + (y1 ? fy : 0.f);
+        c[z] = fmaf(cx, cy, c[z]);
+      }
+    }
+  }
+
+  const long long sx = vol.NX, sxy = (long long)vol.NX * vol.NY;
+  const long long base = (long long)(X0 + tx - vol.Xs) + (long long)(Y0 + ty - vol.Ys) * sx;
+#pragma unroll
+  for (int z = 0; z < kZR; ++z) {
+    const int zz = Z0 + z;
+    if (zz >= z1) break;
+    const long long vi = base + (long long)(zz - z0) * sxy;
+    float out;
+    if (MODE == 0) {
+      out = (c[z] != 0.f) ? s[z] / c[z] : 0.f;
+      vol_out[vi] = out;
+      cbp[vi] = c[z];
+    } else if (MODE == 1) {
+      const float cv = cbp[vi];
+      out = vol_out[vi];
+      if (cv != 0.f) {
+        out = fmaf(step, s[z] / cv, out);
+        vol_out[vi] = out;
+      }
+    } else {
+      cbp[vi] = c[z];
+      continue;
+    }
+    if (copy_kind == 1) static_cast<__nv_bfloat16*>(vol_copy)[vi] = __float2bfloat16_rn(out);
+    else if (copy_kind == 2) static_cast<__half*>(vol_copy)[vi] = __float2half_rn(out);
+  }
+}
+
+// Voxel-driven bilinear splat (FunctionOnGPU.cu:27-52, 316-333) into s.
+// x == nullptr splats ones (row sums c = A 1).
+template <typename VT>
+__global__ void __launch_bounds__(kTX * kTY)
+fwd_splat_kernel(AxisDev ax, VolDev vol, const VT* __restrict__ x, float* __restrict__ s, int z0, int z1) {
+  extern __shared__ AngleConst sk[];
+  const int tid = threadIdx.x + threadIdx.y * kTX;
+  const int X0 = vol.Xs + blockIdx.x * kTX;
+  const int Y0 = vol.Ys + blockIdx.y * kTY;
+  const int Z0 = z0 + blockIdx.z * kZR;
+  for (int a = tid; a < ax.A; a += kTX * kTY) make_angle_const(ax.xc, ax.yc, a, X0, Y0, Z0, sk[a]);
+  __syncthreads();
+
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  if (X0 + tx >= vol.Xs + vol.NX || Y0 + ty >= vol.Ys + vol.NY) return;
+  const int PX = ax.PX, PY = ax.PY;
+  const long long plane = (long long)PX * PY;
+
+  const long long sx = vol.NX, sxy = (long long)vol.NX * vol.NY;
+  const long long base = (long long)(X0 + tx - vol.Xs) + (long long)(Y0 + ty - vol.Ys) * sx;
+  float v[kZR];
+#pragma unroll
+  for (int z = 0; z < kZR; ++z) {
+    const int zz = Z0 + z;
+    v[z] = 0.f;
+    if (zz < z1) v[z] = x ? ld_f(x + base + (long long)(zz - z0) * sxy) : 1.f;
+  }
+
+  for (int a = 0; a < ax.A; ++a) {
+    const AngleConst k = sk[a];
+    const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
+    const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
+    float* sp = s + plane * a;
+#pragma unroll
+    for (int z = 0; z < kZR; ++z) {
+      if (Z0 + z >= z1) break;
+      const float xx = fmaf(k.a3, (float)z, xr);
+      const float yy = fmaf(k.b3, (float)z, yr);
+      const float flx = floorf(xx), fly = floorf(yy);
+      const float fx = xx - flx, fy = yy - fly;
+      const int ix = k.xi + (int)flx, iy = k.yi + (int)fly;
+      const bool x0 = (unsigned)ix < (unsigned)PX, x1 = (unsigned)(ix + 1) < (unsigned)PX;
+      const bool y0 = (unsigned)iy < (unsigned)PY, y1 = (unsigned)(iy + 1) < (unsigned)PY;
+      const float g0 = (1.f - fy) * v[z], g1 = fy * v[z];
+      float* row0 = sp + (long long)iy * PX + ix;
+      if (x0 && y0) atomicAdd(row0, (1.f - fx) * g0);
+      if (x1 && y0) atomicAdd(row0 + 1, fx * g0);
+      if (x0 && y1) atomicAdd(row0 + PX, (1.f - fx) * g1);
+      if (x1 && y1) atomicAdd(row0 + PX + 1, fx * g1);
+    }
+  }
+}
+
+// Residual (FunctionOnGPU.cu:228-236): r = b - s/c where c != 0, else b;
+// resets s to zero for the next forward pass; FP64 sum of r^2.
+template <typename BT, typename RT>
+__global__ void __launch_bounds__(256)
+residual_kernel(long long n, const BT* __restrict__ b, float* __restrict__ s, const float* __restrict__ c,
+                RT* __restrict__ r, double* __restrict__ norm2) {
+  double acc = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float sv = s[i];
+    const float cv = c[i];
+    if (cv != 0.f) sv = sv / cv;
+    const float rv = ld_f(b + i) - sv;
+    r[i] = from_f<RT>(rv);
+    s[i] = 0.f;
+    acc += (double)rv * (double)rv;
+  }
+  if (norm2) {
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ double red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+      atomicAdd(norm2, t);
+    }
+  }
+}
+
+dim3 vol_grid(const VolDev& vol, int z0, int z1) {
+  return dim3((vol.NX + kTX - 1) / kTX, (vol.NY + kTY - 1) / kTY, (z1 - z0 + kZR - 1) / kZR);
+}
+
+}  // namespace
+
+template <typename PT>
+void launch_backproject(const AxisDev& ax, const VolDev& vol, const PT* img, int mode, float step,
+                        float* vol_out, float* cbp, void* vol_copy, int copy_kind, int z0, int z1,
+                        cudaStream_t st) {
+  const dim3 grid = vol_grid(vol, z0, z1), block(kTX, kTY);
+  const size_t smem = sizeof(AngleConst) * ax.A;
+  if (mode == 0)
+    bp_gather_kernel<PT, 0><<<grid, block, smem, st>>>(ax, vol, img, step, vol_out, cbp, vol_copy, copy_kind, z0, z1);
+  else if (mode == 1)
+    bp_gather_kernel<PT, 1><<<grid, block, smem, st>>>(ax, vol, img, step, vol_out, cbp, vol_copy, copy_kind, z0, z1);
+  else
+    bp_gather_kernel<PT, 2><<<grid, block, smem, st>>>(ax, vol, img, step, vol_out, cbp, vol_copy, copy_kind, z0, z1);
+}
+
+template <typename VT>
+void launch_forward(const AxisDev& ax, const VolDev& vol, const VT* x, float* s, int z0, int z1, cudaStream_t st) {
+  const dim3 grid = vol_grid(vol, z0, z1), block(kTX, kTY);
+  const size_t smem = sizeof(AngleConst) * ax.A;
+  fwd_splat_kernel<VT><<<grid, block, smem, st>>>(ax, vol, x, s, z0, z1);
+}
+
+template <typename BT, typename RT>
+void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, double* norm2, cudaStream_t st) {
+  long long blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks < 1) blocks = 1;
+  residual_kernel<BT, RT><<<(unsigned)blocks, 256, 0, st>>>(n, b, s, c, r, norm2);
+}
+
+template void launch_backproject<float>(const AxisDev&, const VolDev&, const float*, int, float, float*, float*,
+                                        void*, int, int, int, cudaStream_t);
+template void launch_backproject<__half>(const AxisDev&, const VolDev&, const __half*, int, float, float*, float*,
+                                         void*, int, int, int, cudaStream_t);
+template void launch_forward<float>(const AxisDev&, const VolDev&, const float*, float*, int, int, cudaStream_t);
+template void launch_forward<__nv_bfloat16>(const AxisDev&, const VolDev&, const __nv_bfloat16*, float*, int, int,
+                                            cudaStream_t);
+template void launch_forward<__half>(const AxisDev&, const VolDev&, const __half*, float*, int, int, cudaStream_t);
+template void launch_residual<float, float>(long long, const float*, float*, const float*, float*, double*,
+                                            cudaStream_t);
+template void launch_residual<__half, __half>(long long, const __half*, float*, const float*, __half*, double*,
+                                              cudaStream_t);
+
+}  // namespace mtr

@@ -1,0 +1,366 @@
+// Device-resident multi-axis reconstruction (WBP init -> SIRT -> MACE) and the
+// C ABI entry points that replace the reference's host functions.
+//
+// Reference flow being replaced (one MPI rank per GPU, host round trips):
+//   ComputeInitialModel + Gatherv/Reduce  (FunctionOnGPU.cu:138-179, MultiAxis.cpp:172-200)
+//   reconstructModel                      (MultiAxis.cpp:40-71)
+//     initialZdata, Scatterv, runSIRTOnGPU, Gatherv, runMaceOnCPU, Reduce/Bcast
+// Here every array stays in HBM for the whole run; each SIRT iteration is
+// three launches per axis (forward splat, residual, back-projection update)
+// and each MACE iteration ends with one fused launch over all axes.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+
+#include "mtr_internal.h"
+#include "mtr_runtime.h"
+
+using namespace mtr;
+
+mtr_recon::~mtr_recon() {
+  if (graph) cudaGraphExecDestroy(graph);
+}
+
+namespace {
+
+int copy_kind_of(int precision) {
+  if (precision == MTR_PREC_MIXED_BF16) return 1;
+  if (precision == MTR_PREC_MIXED_FP16) return 2;
+  return 0;
+}
+
+bool mixed(int precision) { return precision != MTR_PREC_FP32; }
+
+long long axis_bytes(long long np, long long nv, int precision) {
+  const long long pe = mixed(precision) ? 2 : 4;
+  long long b = 0;
+  b += np * pe;       // b
+  b += np * 4;        // s
+  b += np * 4;        // cf
+  b += np * pe;       // r
+  b += nv * 4 * 3;    // cbp, w, x
+  if (mixed(precision)) b += nv * 2;  // xcopy
+  return b;
+}
+
+mtr_status check_params(mtr_context* ctx, const mtr_params& p) {
+  if (p.iter_times < 0 || p.sirt_inner < 0) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "negative iteration count");
+  if (p.precision < MTR_PREC_FP32 || p.precision > MTR_PREC_MIXED_FP16)
+    return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "unknown precision");
+  if (!std::isfinite(p.sirt_step) || !std::isfinite(p.mace_step))
+    return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "non-finite step");
+  return MTR_OK;
+}
+
+mtr_status upload_projections(mtr_recon* r, int k, const float* data, int mem_kind) {
+  mtr_context* ctx = r->ctx;
+  AxisState& a = r->ax[k];
+  const size_t fbytes = (size_t)a.np * sizeof(float);
+  const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (!mixed(r->p.precision)) {
+    MTR_CK(ctx, cudaMemcpyAsync(a.b.p, data, fbytes, kind, ctx->stream));
+    return MTR_OK;
+  }
+  // Mixed: stage as float in the forward accumulator, convert to fp16.
+  MTR_CK(ctx, cudaMemcpyAsync(a.s.p, data, fbytes, kind, ctx->stream));
+  launch_convert_copy(a.s.as<float>(), a.b.p, 2, a.np, ctx->stream);
+  MTR_CK_LAUNCH(ctx, "convert projections");
+  MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, fbytes, ctx->stream));
+  return MTR_OK;
+}
+
+// Geometry-only arrays: forward row sums cf = A 1.  (cbp is produced by WBP.)
+mtr_status enqueue_geometry(mtr_recon* r) {
+  mtr_context* ctx = r->ctx;
+  const VolDev& v = r->vol;
+  for (auto& a : r->ax) {
+    MTR_CK(ctx, cudaMemsetAsync(a.cf.p, 0, (size_t)a.np * 4, ctx->stream));
+    launch_forward<float>(a.dev(), v, nullptr, a.cf.as<float>(), v.Zs, v.Zs + v.NZ, ctx->stream);
+    MTR_CK_LAUNCH(ctx, "forward row sums");
+  }
+  return MTR_OK;
+}
+
+mtr_status enqueue_forward(mtr_recon* r, AxisState& a) {
+  mtr_context* ctx = r->ctx;
+  const VolDev& v = r->vol;
+  const int z0 = v.Zs, z1 = v.Zs + v.NZ;
+  switch (copy_kind_of(r->p.precision)) {
+    case 1: launch_forward<__nv_bfloat16>(a.dev(), v, a.xcopy.as<__nv_bfloat16>(), a.s.as<float>(), z0, z1, ctx->stream); break;
+    case 2: launch_forward<__half>(a.dev(), v, a.xcopy.as<__half>(), a.s.as<float>(), z0, z1, ctx->stream); break;
+    default: launch_forward<float>(a.dev(), v, a.x.as<float>(), a.s.as<float>(), z0, z1, ctx->stream); break;
+  }
+  MTR_CK_LAUNCH(ctx, "forward splat");
+  return MTR_OK;
+}
+
+mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
+  mtr_context* ctx = r->ctx;
+  if (mixed(r->p.precision))
+    launch_residual<__half, __half>(a.np, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<__half>(), norm,
+                                    ctx->stream);
+  else
+    launch_residual<float, float>(a.np, a.b.as<float>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), norm,
+                                  ctx->stream);
+  MTR_CK_LAUNCH(ctx, "residual");
+  return MTR_OK;
+}
+
+mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const void* img_f32_or_null) {
+  mtr_context* ctx = r->ctx;
+  const VolDev& v = r->vol;
+  const int z0 = v.Zs, z1 = v.Zs + v.NZ;
+  const int ck = copy_kind_of(r->p.precision);
+  if (mixed(r->p.precision)) {
+    const __half* img = mode == 0 ? a.b.as<__half>() : a.r.as<__half>();
+    launch_backproject<__half>(a.dev(), v, img, mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(),
+                               a.xcopy.p, ck, z0, z1, ctx->stream);
+  } else {
+    const float* img = mode == 0 ? a.b.as<float>() : a.r.as<float>();
+    if (img_f32_or_null) img = static_cast<const float*>(img_f32_or_null);
+    launch_backproject<float>(a.dev(), v, img, mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(), nullptr, 0,
+                              z0, z1, ctx->stream);
+  }
+  MTR_CK_LAUNCH(ctx, mode == 0 ? "wbp" : "sirt back-projection");
+  return MTR_OK;
+}
+
+// WBP init, w_k = z_k = x0 sum, then the MACE loop.
+mtr_status enqueue_run(mtr_recon* r) {
+  mtr_context* ctx = r->ctx;
+  const long long nv = r->nv;
+  const size_t vbytes = (size_t)nv * 4;
+  const int ck = copy_kind_of(r->p.precision);
+  float* wavg = r->wavg.as<float>();
+  // Initial model: sum over axes of each axis' WBP (MultiAxis.cpp:181-200).
+  MTR_CK(ctx, cudaMemsetAsync(wavg, 0, vbytes, ctx->stream));
+  for (auto& a : r->ax) {
+    mtr_status s = enqueue_bp(r, a, 0, nullptr);
+    if (s != MTR_OK) return s;
+    launch_axpy_acc(wavg, a.x.as<float>(), nv, ctx->stream);
+    MTR_CK_LAUNCH(ctx, "initial model sum");
+  }
+  // w_k = w_avg; first z_k = 2 w_avg - w_k = w_avg.
+  for (auto& a : r->ax) {
+    MTR_CK(ctx, cudaMemcpyAsync(a.w.p, wavg, vbytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (ck) {
+      launch_convert_copy(wavg, a.xcopy.p, ck, nv, ctx->stream);
+      MTR_CK_LAUNCH(ctx, "volume copy");
+    }
+  }
+  const int K = r->K, ni = r->p.sirt_inner, no = r->p.iter_times;
+  double* norms = r->norms.as<double>();
+  double* dch = r->dchange.as<double>();
+  if (norms) MTR_CK(ctx, cudaMemsetAsync(norms, 0, sizeof(double) * (size_t)no * K * ni, ctx->stream));
+  if (dch) MTR_CK(ctx, cudaMemsetAsync(dch, 0, sizeof(double) * (size_t)no, ctx->stream));
+  std::vector<float*> ws(K), xs(K);
+  std::vector<void*> xcs(K);
+  for (int k = 0; k < K; ++k) {
+    ws[k] = r->ax[k].w.as<float>();
+    xs[k] = r->ax[k].x.as<float>();
+    xcs[k] = r->ax[k].xcopy.p;
+  }
+  for (int it = 0; it < no; ++it) {
+    for (int k = 0; k < K; ++k) {
+      AxisState& a = r->ax[k];
+      for (int j = 0; j < ni; ++j) {
+        mtr_status s = enqueue_forward(r, a);
+        if (s != MTR_OK) return s;
+        s = enqueue_residual(r, a, norms ? norms + ((long long)it * K + k) * ni + j : nullptr);
+        if (s != MTR_OK) return s;
+        s = enqueue_bp(r, a, 1, nullptr);
+        if (s != MTR_OK) return s;
+      }
+    }
+    launch_mace(K, ws.data(), xs.data(), wavg, nv, r->p.mace_step, xcs.data(), ck, dch ? dch + it : nullptr,
+                ctx->stream);
+    MTR_CK_LAUNCH(ctx, "mace");
+  }
+  return MTR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mtr_status mtr_estimate_footprint(int n_axes, const mtr_projection_size* prjs, mtr_volume_size vol, int precision,
+                                  long long* bytes) {
+  if (!bytes || n_axes <= 0 || !prjs) return MTR_ERR_INVALID_ARGUMENT;
+  const long long nv = (long long)vol.X * vol.Y * vol.Z;
+  long long b = nv * 4;  // wavg
+  for (int k = 0; k < n_axes; ++k) {
+    const long long np = (long long)prjs[k].X * prjs[k].Y * prjs[k].AngN;
+    b += axis_bytes(np, nv, precision) + 64LL * prjs[k].AngN;
+  }
+  *bytes = b;
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
+                            const mtr_params* params, int mem_kind, mtr_recon** out) {
+  if (!ctx || !out || !axes || !params) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "null argument");
+  *out = nullptr;
+  if (n_axes <= 0 || n_axes > MTR_MAX_AXES) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "axis count out of range");
+  if (mem_kind != MTR_MEM_HOST && mem_kind != MTR_MEM_DEVICE)
+    return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  mtr_status s = check_volume(ctx, vol);
+  if (s != MTR_OK) return s;
+  s = check_params(ctx, *params);
+  if (s != MTR_OK) return s;
+  for (int k = 0; k < n_axes; ++k) {
+    s = check_axis(ctx, axes[k]);
+    if (s != MTR_OK) return s;
+  }
+  DeviceGuard g(ctx->device);
+  std::unique_ptr<mtr_recon> r(new (std::nothrow) mtr_recon());
+  if (!r) return set_error(ctx, MTR_ERR_OUT_OF_MEMORY, "host allocation");
+  r->ctx = ctx;
+  r->vs = vol;
+  r->vol = VolDev{vol.Xstart, vol.Ystart, vol.Zstart, vol.X, vol.Y, vol.Z};
+  r->p = *params;
+  r->K = n_axes;
+  r->nv = (long long)vol.X * vol.Y * vol.Z;
+  r->ax.resize(n_axes);
+  const bool mx = mixed(params->precision);
+  const size_t vb = (size_t)r->nv * 4;
+  MTR_CK(ctx, r->wavg.alloc(vb));
+  r->bytes += vb;
+  for (int k = 0; k < n_axes; ++k) {
+    AxisState& a = r->ax[k];
+    a.PX = axes[k].prj.X;
+    a.PY = axes[k].prj.Y;
+    a.A = axes[k].prj.AngN;
+    a.np = (long long)a.PX * a.PY * a.A;
+    const size_t pe = mx ? 2 : 4;
+    MTR_CK(ctx, a.xc.alloc(sizeof(double) * 4 * a.A));
+    MTR_CK(ctx, a.yc.alloc(sizeof(double) * 4 * a.A));
+    MTR_CK(ctx, a.b.alloc((size_t)a.np * pe));
+    MTR_CK(ctx, a.s.alloc((size_t)a.np * 4));
+    MTR_CK(ctx, a.cf.alloc((size_t)a.np * 4));
+    MTR_CK(ctx, a.r.alloc((size_t)a.np * pe));
+    MTR_CK(ctx, a.cbp.alloc(vb));
+    MTR_CK(ctx, a.w.alloc(vb));
+    MTR_CK(ctx, a.x.alloc(vb));
+    if (mx) MTR_CK(ctx, a.xcopy.alloc((size_t)r->nv * 2));
+    r->bytes += axis_bytes(a.np, r->nv, params->precision) + 64LL * a.A;
+    MTR_CK(ctx, cudaMemcpyAsync(a.xc.p, axes[k].x_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
+    MTR_CK(ctx, cudaMemcpyAsync(a.yc.p, axes[k].y_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
+    MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream));
+    s = upload_projections(r.get(), k, axes[k].prj_data, mem_kind);
+    if (s != MTR_OK) return s;
+  }
+  if (params->flags & MTR_FLAG_RECORD_NORMS) {
+    const size_t n = (size_t)std::max(1, params->iter_times) * n_axes * std::max(1, params->sirt_inner);
+    MTR_CK(ctx, r->norms.alloc(sizeof(double) * n));
+    MTR_CK(ctx, r->dchange.alloc(sizeof(double) * std::max(1, params->iter_times)));
+  }
+  s = enqueue_geometry(r.get());
+  if (s != MTR_OK) return s;
+  r->geometry_ready = true;
+  // Host staging buffers passed in may be freed after return: finish the copies.
+  MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = r.release();
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_upload(mtr_recon* r, int axis, const float* prj_data, int mem_kind) {
+  if (!r || !prj_data || axis < 0 || axis >= r->K) return MTR_ERR_INVALID_ARGUMENT;
+  DeviceGuard g(r->ctx->device);
+  return upload_projections(r, axis, prj_data, mem_kind);
+}
+
+mtr_status mtr_recon_run(mtr_recon* r) {
+  if (!r) return MTR_ERR_INVALID_ARGUMENT;
+  mtr_context* ctx = r->ctx;
+  DeviceGuard g(ctx->device);
+  if (!(r->p.flags & MTR_FLAG_GRAPH)) return enqueue_run(r);
+  if (!r->graph) {
+    cudaGraph_t graph = nullptr;
+    MTR_CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    const long long before = g_launches.load();
+    mtr_status s = enqueue_run(r);
+    const long long nodes = g_launches.load() - before;
+    g_launches.fetch_sub(nodes);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (s != MTR_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return s;
+    }
+    if (e != cudaSuccess) return cuda_error(ctx, e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&r->graph, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      r->graph = nullptr;
+      return cuda_error(ctx, e, "cudaGraphInstantiate");
+    }
+    r->graph_nodes = nodes;
+  }
+  MTR_CK(ctx, cudaGraphLaunch(r->graph, ctx->stream));
+  g_launches.fetch_add(r->graph_nodes);
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_download(mtr_recon* r, float* out, int mem_kind) {
+  if (!r || !out) return MTR_ERR_INVALID_ARGUMENT;
+  mtr_context* ctx = r->ctx;
+  DeviceGuard g(ctx->device);
+  const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  MTR_CK(ctx, cudaMemcpyAsync(out, r->wavg.p, (size_t)r->nv * 4, kind, ctx->stream));
+  if (mem_kind != MTR_MEM_DEVICE) MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind) {
+  if (!r || !out) return MTR_ERR_INVALID_ARGUMENT;
+  mtr_context* ctx = r->ctx;
+  DeviceGuard g(ctx->device);
+  const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  for (int k = 0; k < r->K; ++k)
+    MTR_CK(ctx, cudaMemcpyAsync(out + (size_t)k * r->nv, r->ax[k].w.p, (size_t)r->nv * 4, kind, ctx->stream));
+  if (mem_kind != MTR_MEM_DEVICE) MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n) {
+  if (!r || !out) return MTR_ERR_INVALID_ARGUMENT;
+  if (!r->norms.p) return set_error(r->ctx, MTR_ERR_INVALID_ARGUMENT, "norms not recorded (MTR_FLAG_RECORD_NORMS)");
+  const long long have = (long long)r->p.iter_times * r->K * r->p.sirt_inner;
+  if (n > have) n = have;
+  DeviceGuard g(r->ctx->device);
+  MTR_CK(r->ctx, cudaMemcpyAsync(out, r->norms.p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, r->ctx->stream));
+  MTR_CK(r->ctx, cudaStreamSynchronize(r->ctx->stream));
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_footprint(const mtr_recon* r, long long* bytes) {
+  if (!r || !bytes) return MTR_ERR_INVALID_ARGUMENT;
+  *bytes = r->bytes;
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_destroy(mtr_recon* r) {
+  if (!r) return MTR_OK;
+  DeviceGuard g(r->ctx->device);
+  cudaStreamSynchronize(r->ctx->stream);
+  delete r;
+  return MTR_OK;
+}
+
+// ---- Reference-shaped entry points (host buffers in and out) --------------
+
+mtr_status mtr_reconstruct(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
+                           const mtr_params* params, float* out_volume) {
+  if (!ctx || !out_volume) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "null argument");
+  mtr_recon* r = nullptr;
+  mtr_status s = mtr_recon_create(ctx, n_axes, axes, vol, params, MTR_MEM_HOST, &r);
+  if (s != MTR_OK) return s;
+  s = mtr_recon_run(r);
+  if (s == MTR_OK) s = mtr_recon_download(r, out_volume, MTR_MEM_HOST);
+  mtr_recon_destroy(r);
+  return s;
+}
+
+}  // extern "C"

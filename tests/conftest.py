@@ -1,0 +1,39 @@
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+PKG = ROOT / "multi-tilt-reconstuction_gb300"
+for p in (ROOT, PKG, ROOT / "oracle", ROOT / "tests"):
+    if str(p) not in sys.path:
+        sys.path.insert(0, str(p))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session", autouse=True)
+def built():
+    import __graft_entry__
+
+    __graft_entry__.build()
+    return True
+
+
+@pytest.fixture(scope="session")
+def ctx(built):
+    import mtr
+
+    c = mtr.Context(0)
+    yield c
+    c.close()
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    n = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (n if n > 0 else 1.0))

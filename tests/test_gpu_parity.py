@@ -1,0 +1,147 @@
+"""GPU parity: libmtr (through its C ABI) against the CPU oracle and, where
+the prebuilt cubin is present, against the reference's own CUDA kernels.
+
+Bounds (relative L2 per volume):
+  FP32 path vs reference-faithful oracle / reference kernels: 1e-4
+  mixed precision vs the FP64 oracle:                          1e-3
+"""
+import numpy as np
+import pytest
+
+import cases
+import mtr
+import oracle
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FP32_TOL = 1e-4
+MIXED_TOL = 1e-3
+
+
+@pytest.mark.parametrize("name", ["single", "two_axis", "oob", "four_axis", "rect"])
+def test_wbp_matches_oracle(ctx, name):
+    c = cases.get(name)
+    for a in c.axes:
+        got = ctx.wbp(a, c.vol)
+        want = oracle.wbp(oracle.REF_FAITHFUL, a, c.vol)
+        assert rel_l2(got, want) < 1e-5
+
+
+def test_wbp_slab_matches_full_volume(ctx):
+    c = cases.get("single")
+    v = c.vol
+    full = ctx.wbp(c.axes[0], v)
+    lo = ctx.wbp(c.axes[0], v, v.Zstart, v.Zstart + 3)
+    hi = ctx.wbp(c.axes[0], v, v.Zstart + 3, v.Zend)
+    # Not bit-identical: each CTA evaluates the map in FP64 at its own base
+    # voxel, and the slab origin moves that base.
+    assert rel_l2(np.concatenate([lo, hi]), full) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["single", "oob", "rect"])
+def test_sirt_matches_oracle(ctx, name):
+    c = cases.get(name)
+    a = c.axes[0]
+    x0 = oracle.wbp(oracle.REF_FAITHFUL, a, c.vol).astype(np.float32)
+    got = ctx.sirt(a, c.vol, x0, n_inner=6, step=0.5)
+    want = oracle.sirt(oracle.REF_FAITHFUL, a, c.vol, x0, 6, 0.5)
+    assert rel_l2(got, want) < FP32_TOL
+
+
+@pytest.mark.parametrize("name,no,ni,rho", [("single", 1, 10, 0.5), ("two_axis", 2, 3, 0.8),
+                                            ("four_axis", 2, 2, 0.7), ("oob", 1, 3, 0.7)])
+def test_reconstruct_matches_oracle(ctx, name, no, ni, rho):
+    c = cases.get(name)
+    p = mtr.params(iter_times=no, sirt_inner=ni, sirt_step=0.5, mace_step=rho)
+    got = ctx.reconstruct(c.axes, c.vol, p)
+    want = oracle.reconstruct(oracle.REF_FAITHFUL, c.axes, c.vol, no, ni, 0.5, rho)
+    assert rel_l2(got, want) < FP32_TOL
+
+
+@pytest.mark.parametrize("prec", [mtr.PREC_MIXED_BF16, mtr.PREC_MIXED_FP16])
+def test_mixed_precision_vs_fp64(ctx, prec):
+    c = cases.get("two_axis")
+    p = mtr.params(iter_times=2, sirt_inner=4, sirt_step=0.5, mace_step=0.8, precision=prec)
+    got = ctx.reconstruct(c.axes, c.vol, p)
+    want = oracle.reconstruct(oracle.FP64, c.axes, c.vol, 2, 4, 0.5, 0.8)
+    assert rel_l2(got, want) < MIXED_TOL
+
+
+def test_graph_replay_matches_direct(ctx):
+    c = cases.get("two_axis")
+    p = mtr.params(iter_times=2, sirt_inner=3, sirt_step=0.5, mace_step=0.8)
+    direct = ctx.reconstruct(c.axes, c.vol, p)
+    pg = mtr.params(iter_times=2, sirt_inner=3, sirt_step=0.5, mace_step=0.8, flags=mtr.FLAG_GRAPH)
+    r = mtr.Recon(ctx, c.axes, c.vol, pg)
+    r.run()
+    first = r.download()
+    r.run()  # replay
+    second = r.download()
+    r.close()
+    assert rel_l2(first, direct) < 1e-5
+    assert rel_l2(second, first) < 1e-5
+
+
+def test_residual_norms_decrease_and_match_oracle(ctx):
+    c = cases.get("single")
+    p = mtr.params(iter_times=1, sirt_inner=8, sirt_step=0.5, mace_step=0.5, flags=mtr.FLAG_RECORD_NORMS)
+    r = mtr.Recon(ctx, c.axes, c.vol, p)
+    r.run()
+    n = r.norms()[0, 0]
+    r.close()
+    _, want = oracle.reconstruct(oracle.FP64, c.axes, c.vol, 1, 8, 0.5, 0.5, with_norms=True)
+    assert np.all(np.diff(n) < 0)
+    np.testing.assert_allclose(n, want[0, 0], rtol=1e-4)
+
+
+def test_elementwise_bit_exact(ctx):
+    rng = np.random.default_rng(5)
+    v = mtr.VolumeSize.make(0, 17, 0, 9, 0, 3)
+    w = rng.normal(size=v.shape).astype(np.float32)
+    wa = rng.normal(size=v.shape).astype(np.float32)
+    z = ctx.initial_z(v, w, wa)
+    np.testing.assert_array_equal(z, (np.float32(2) * wa - w).astype(np.float32))
+    vv = rng.normal(size=v.shape).astype(np.float32)
+    step = np.float32(0.7)
+    got = ctx.update_w(v, vv, z, w, float(step))
+    want = step * (np.float32(2) * vv - z) + (np.float32(1) - step) * w
+    np.testing.assert_array_equal(got, want.astype(np.float32))
+
+
+def test_invalid_arguments_do_not_poison_context(ctx):
+    c = cases.get("single")
+    bad = mtr.VolumeSize(0, 10, 0, 10, 0, 10, 9, 10, 10)  # X != Xend - Xstart
+    with pytest.raises(mtr.MtrError) as e:
+        ctx.wbp(c.axes[0], bad)
+    assert e.value.status == mtr.ERR_INVALID_ARGUMENT
+    a = mtr.AxisData(c.axes[0].x_coef.copy(), c.axes[0].y_coef, c.axes[0].data)
+    a.x_coef[3] = np.nan
+    with pytest.raises(mtr.MtrError):
+        ctx.wbp(a, c.vol)
+    # the context still works
+    got = ctx.wbp(c.axes[0], c.vol)
+    assert rel_l2(got, oracle.wbp(0, c.axes[0], c.vol)) < 1e-5
+
+
+# --- the reference's own kernels (cubin built from FunctionOnGPU.cu) ------------------
+
+needs_ref = pytest.mark.skipif(not oracle.refrun_available(), reason="reference cubin not built here")
+
+
+@needs_ref
+@pytest.mark.parametrize("name", ["single", "two_axis", "oob"])
+def test_wbp_matches_reference_kernels(ctx, name):
+    c = cases.get(name)
+    a = c.axes[0]
+    assert rel_l2(ctx.wbp(a, c.vol), oracle.ref_wbp(a, c.vol)) < 1e-5
+
+
+@needs_ref
+@pytest.mark.parametrize("name,no,ni,rho", [("single", 1, 10, 0.5), ("two_axis", 2, 3, 0.8)])
+def test_reconstruct_matches_reference_kernels(ctx, name, no, ni, rho):
+    c = cases.get(name)
+    p = mtr.params(iter_times=no, sirt_inner=ni, sirt_step=0.5, mace_step=rho)
+    got = ctx.reconstruct(c.axes, c.vol, p)
+    want = oracle.ref_reconstruct(c.axes, c.vol, no, ni, 0.5, rho)
+    assert rel_l2(got, want) < FP32_TOL
