@@ -1,0 +1,419 @@
+#!/usr/bin/env python
+"""Benchmark: multi-axis SIRT + MACE reconstruction, voxel-updates/s on GB300.
+
+One step = one complete reconstruction of the workload (per-axis WBP init,
+n_outer MACE iterations of n_inner SIRT iterations per axis, consensus),
+with inputs resident in HBM.  voxel-updates per step = V * K * n_outer * n_inner.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2] [--impl ours|reference]
+
+The default workload is the 3-axis 512x512x128 MACE configuration; the
+headline value is the mixed-precision path (BF16 volume copy, FP16
+projections/residuals, FP32 interpolation/accumulation, FP64 norms and
+consensus), with the plain FP32 path timed beside it.  Multi-GPU runs are
+independent replicas (the reconstruction is not sharded across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "multi-tilt-reconstuction_gb300"
+for p in (str(PKG), str(ROOT / "oracle"), str(ROOT)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+METRIC = "SIRT voxel-updates/s mixed vs FP32 @<=1e-3 rel-L2 vs FP64"
+UNIT = "voxel-updates/s"
+
+CONFIGS = {
+    "c1": dict(workload="single-axis SIRT 128x128x32, 61 tilts (+-60 step 2) x 128^2 px, WBP + 10 SIRT, lambda 0.5",
+               vol=(0, 128, 0, 128, 0, 32), px=128, tilts=(-60, 61, 2), phis=(0.0,), n_ell=20,
+               noise=("gaussian", 0.02), seed=1001, n_outer=1, n_inner=10, sirt_step=0.5, mace_step=0.5),
+    "c2": dict(workload="3-axis MACE 512x512x128, axes 0/60/120 deg, 61 tilts (+-60 step 2) x 512^2 px, "
+                        "2 MACE x 10 SIRT per axis, lambda 0.5, rho 0.8",
+               vol=(0, 512, 0, 512, 0, 128), px=512, tilts=(-60, 61, 2), phis=(0.0, 60.0, 120.0), n_ell=50,
+               noise=("gaussian", 0.05), seed=1002, n_outer=2, n_inner=10, sirt_step=0.5, mace_step=0.8),
+    "c3": dict(workload="4-axis 2048x2048x256, axes 0/45/90/135 deg, 121 tilts (+-60 step 1) x 2048^2 px, "
+                        "3 MACE x 10 SIRT per axis, lambda 0.5, rho 0.7, Poisson dose 50",
+               vol=(0, 2048, 0, 2048, 0, 256), px=2048, tilts=(-60, 61, 1), phis=(0.0, 45.0, 90.0, 135.0), n_ell=200,
+               noise=("poisson", 50.0), seed=1003, n_outer=3, n_inner=10, sirt_step=0.5, mace_step=0.7),
+}
+
+
+def peaks() -> tuple[dict, str]:
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        return json.loads(f.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def voxel_updates(cfg: dict) -> int:
+    v = cfg["vol"]
+    V = (v[1] - v[0]) * (v[3] - v[2]) * (v[5] - v[4])
+    return V * len(cfg["phis"]) * cfg["n_outer"] * cfg["n_inner"]
+
+
+def n_angles(cfg: dict) -> int:
+    return len(range(*cfg["tilts"]))
+
+
+# ----------------------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self) -> None:
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self) -> None:
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------------------
+def make_inputs(cfg: dict, device: str):
+    import mtr
+    import phantom
+
+    vol = mtr.VolumeSize.make(*cfg["vol"])
+    tilts = np.arange(*cfg["tilts"], dtype=np.float64)
+    kind, level = cfg["noise"]
+    case = phantom.make_case_torch(vol, cfg["px"], tilts, list(cfg["phis"]), cfg["n_ell"], kind, level, cfg["seed"],
+                                   device=device)
+    axes = [mtr.AxisData(xc, yc, d) for (xc, yc, d) in case["axes"]]
+    return vol, axes, case["meta"]
+
+
+def time_steps(torch, stream, recon, steps: int) -> float:
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    start.record(stream)
+    for _ in range(steps):
+        recon.run()
+    end.record(stream)
+    end.synchronize()
+    return start.elapsed_time(end) / steps
+
+
+def algorithmic_bytes(kind: str, cfg: dict, prec: int) -> tuple[float, str]:
+    """Compulsory HBM bytes of one launch of a kernel class (one axis)."""
+    import mtr
+
+    v = cfg["vol"]
+    V = (v[1] - v[0]) * (v[3] - v[2]) * (v[5] - v[4])
+    P = cfg["px"] * cfg["px"] * n_angles(cfg)
+    pe = 2 if prec != mtr.PREC_FP32 else 4
+    if kind == "backproject":
+        # read r (P), read+write the FP32 iterate, read the weight sums (+ write the bf16 copy when mixed)
+        b = P * pe + V * 12 + (V * 2 if prec != mtr.PREC_FP32 else 0)
+        return b, f"P*{pe} (residual) + V*12 (iterate r/w, weight sums){' + V*2 (bf16 copy)' if pe == 2 else ''}"
+    if kind == "forward":
+        vb = 2 if prec != mtr.PREC_FP32 else 4
+        return P * 4 + V * vb, f"V*{vb} (volume read) + P*4 (ray-sum write)"
+    if kind == "residual":
+        return P * (4 + 4 + 4 + pe + pe), f"P*(s r/w 8 + c 4 + b {pe} + r {pe})"
+    if kind == "mace":
+        K = len(cfg["phis"])
+        return V * 4 * (2 + 4 * K), "V*4*(2 + 4K) (w_avg r/w, w_k r/w, x_k r/w)"
+    return 0.0, "n/a"
+
+
+# ----------------------------------------------------------------------------------------
+def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
+    import torch
+
+    import mtr
+
+    cfg = CONFIGS[args.config]
+    torch.cuda.set_device(local_rank)
+    device = f"cuda:{local_rank}"
+    stream = torch.cuda.current_stream()
+    ctx = mtr.Context(local_rank)
+    ctx.set_stream(stream.cuda_stream)
+    t0 = time.time()
+    vol, axes, meta = make_inputs(cfg, device)
+    gen_s = time.time() - t0
+    no, ni = cfg["n_outer"], cfg["n_inner"]
+    prec = {"bf16": mtr.PREC_MIXED_BF16, "fp16": mtr.PREC_MIXED_FP16, "fp32": mtr.PREC_FP32}[args.precision]
+    mk = lambda pr: mtr.params(iter_times=no, sirt_inner=ni, sirt_step=cfg["sirt_step"], mace_step=cfg["mace_step"],
+                               precision=pr)
+    rec = mtr.Recon(ctx, axes, vol, mk(prec), mem_kind=mtr.MEM_DEVICE)
+    ref32 = mtr.Recon(ctx, axes, vol, mk(mtr.PREC_FP32), mem_kind=mtr.MEM_DEVICE) if prec != mtr.PREC_FP32 else rec
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        return float(t.item())
+
+    # warm-up
+    for _ in range(args.warmup):
+        rec.run()
+        if ref32 is not rec:
+            ref32.run()
+    torch.cuda.synchronize()
+
+    # timed region: headline precision, profiled per kernel class, clocks sampled
+    clocks = ClockSampler(local_rank)
+    ctx.profile_reset()
+    ctx.set_profiling(True)
+    launches0 = ctx.launch_count()
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ms = time_steps(torch, stream, rec, args.steps)
+    clk = clocks.stop()
+    launches = ctx.launch_count() - launches0
+    ctx.set_profiling(False)
+    prof = ctx.profile()
+    barrier()
+    ms = max_over_ranks(ms)
+
+    # plain FP32 path, same workload
+    ms32 = time_steps(torch, stream, ref32, args.steps) if ref32 is not rec else ms
+    ms32 = max_over_ranks(ms32)
+
+    out_mixed = rec.download()
+    out_fp32 = ref32.download()
+
+    # end to end through the public host-buffer API: H2D of the projections from
+    # pinned memory, device allocation, geometry sums, the run, D2H of the volume
+    host_axes = []
+    h2d = 0
+    for a in axes:
+        pinned = torch.empty(a.data.shape, dtype=torch.float32, pin_memory=True)
+        pinned.copy_(a.data)
+        host_axes.append(mtr.AxisData(a.x_coef, a.y_coef, pinned.numpy()))
+        h2d += pinned.numel() * 4 + a.x_coef.nbytes + a.y_coef.nbytes
+    out_pinned = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True).numpy()
+    p_e2e = mk(prec)
+    arr_ms = []
+    import ctypes as C
+
+    arr = (mtr.AxisC * len(host_axes))(*[a.c_struct() for a in host_axes])
+    for i in range(1 + max(1, args.e2e_steps)):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ctx.check(ctx.lib.mtr_reconstruct(ctx.h, len(host_axes), arr, vol, C.byref(p_e2e), out_pinned.ctypes.data),
+                  "mtr_reconstruct")
+        dt = time.perf_counter() - t
+        if i > 0:
+            arr_ms.append(dt * 1e3)
+    e2e_ms = max_over_ranks(statistics.mean(arr_ms))
+
+    vu = voxel_updates(cfg)
+    res = {"ms": ms, "ms32": ms32, "e2e_ms": e2e_ms, "h2d": h2d, "d2h": vol.X * vol.Y * vol.Z * 4, "clk": clk,
+           "prof": prof, "launches": launches, "gen_s": gen_s, "meta": meta, "vu": vu,
+           "mixed_vs_fp32": float(np.linalg.norm(out_mixed.astype(np.float64) - out_fp32) /
+                                  max(np.linalg.norm(out_fp32.astype(np.float64)), 1e-30)),
+           "axes_host": host_axes, "vol": vol, "prec": prec}
+    rec.close()
+    if ref32 is not rec:
+        ref32.close()
+    ctx.close()
+    return res
+
+
+def cpu_baseline(cfg: dict, vol, axes_host, budget_s: float = 20.0) -> dict:
+    """Reference-faithful CPU oracle on the host cores: SIRT iterations of axis 0
+    on the full volume (each one = V voxel-updates)."""
+    import oracle
+
+    n = os.cpu_count() or 1
+    oracle.set_threads(n)
+    a = axes_host[0]
+    x0 = np.zeros(vol.shape, np.float64)
+    t = time.perf_counter()
+    it = 0
+    while True:
+        oracle.sirt(oracle.REF_FAITHFUL, a, vol, x0, 1, cfg["sirt_step"])
+        it += 1
+        el = time.perf_counter() - t
+        if el > budget_s / 2 or it >= 3:
+            break
+    V = vol.X * vol.Y * vol.Z
+    return {"value": V * it / el, "unit": UNIT, "cores": n, "kind": "port",
+            "sample": f"{it} reference-faithful SIRT iteration(s) (forward splat + residual + back-projection) of "
+                      f"axis 0 over the full {vol.X}x{vol.Y}x{vol.Z} volume, OpenMP over {n} host threads, "
+                      f"{el:.1f} s"}
+
+
+def run_reference(args) -> dict:
+    """The reference path on the host cores: its own implementation is CUDA+MPI
+    with no CPU version, so the oracle restatement (reference-faithful precision)
+    stands in; one step = one SIRT iteration of axis 0 on the full volume."""
+    import torch
+
+    import mtr
+    import oracle
+
+    cfg = CONFIGS[args.config]
+    vol, axes, _ = make_inputs(cfg, "cuda:0" if torch.cuda.is_available() else "cpu")
+    a = axes[0]
+    host = mtr.AxisData(a.x_coef, a.y_coef, a.data.cpu().numpy() if hasattr(a.data, "cpu") else a.data)
+    n = os.cpu_count() or 1
+    oracle.set_threads(n)
+    x0 = np.zeros(vol.shape, np.float64)
+    for _ in range(args.warmup):
+        oracle.sirt(oracle.REF_FAITHFUL, host, vol, x0, 1, cfg["sirt_step"])
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.sirt(oracle.REF_FAITHFUL, host, vol, x0, 1, cfg["sirt_step"])
+    el = time.perf_counter() - t
+    V = vol.X * vol.Y * vol.Z
+    value = V * args.steps / el
+    return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["workload"], "step": "one SIRT iteration of axis 0 (bounded sample)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": n, "kind": "port",
+                             "sample": f"reference-faithful CPU restatement (the reference's path is CUDA+MPI only), "
+                                       f"one SIRT iteration of axis 0 over the full volume per step, {n} threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(run_reference(args)), flush=True)
+        return 0
+
+    import __graft_entry__
+
+    if rank == 0 or world == 1:
+        __graft_entry__.build()
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl", device_id=torch.device(f"cuda:{local_rank}"))
+        torch.distributed.barrier()
+        if rank != 0:
+            __graft_entry__.build()
+
+    r = run_ours(args, rank, world, local_rank)
+    cfg = CONFIGS[args.config]
+    if rank == 0:
+        import mtr
+
+        pk, pk_kind = peaks()
+        prof = r["prof"]
+        dom = max((k for k in prof if prof[k][0] > 0), key=lambda k: prof[k][1])
+        n_l, tot = prof[dom]
+        per_launch_ms = tot / n_l
+        alg, alg_desc = algorithmic_bytes(dom, cfg, r["prec"])
+        achieved = alg / (per_launch_ms * 1e-3) / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / pk["hbm_gbs"], "traffic": None, "kernel": dom, "peak_source": pk_kind,
+                "algorithmic_bytes_per_launch": alg, "algorithmic_bytes": alg_desc,
+                "avg_launch_ms": per_launch_ms, "launches": n_l,
+                "kernel_share": {k: prof[k][1] / max(sum(x[1] for x in prof.values()), 1e-9) for k in prof}}
+        vu = r["vu"] * world
+        value = vu / (r["ms"] * 1e-3)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": cfg["workload"], "precision": args.precision,
+                       "storage": "bf16 volume copy, fp16 projections/residuals" if args.precision != "fp32"
+                       else "fp32", "voxel_updates_per_step": r["vu"], "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (each volume array 134 MB, projections 64 MB per axis)",
+                       "seed": cfg["seed"]},
+            "fp32": {"value": vu / (r["ms32"] * 1e-3), "ms_per_step": r["ms32"],
+                     "mixed_over_fp32": r["ms32"] / r["ms"]},
+            "error": {"mixed_vs_fp32_rel_l2": r["mixed_vs_fp32"]},
+            "e2e": {"value": vu / (r["e2e_ms"] * 1e-3), "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"],
+                    "api": "mtr_reconstruct (host buffers, pinned)"},
+            "gpu_launches": r["launches"],
+            "roofline": roof,
+            "clocks": r["clk"],
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(cfg, r["vol"], r["axes_host"])
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch
+
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -110,8 +110,25 @@ mtr_status mtr_context_destroy(mtr_context* ctx);
 /* Use an external cudaStream_t (NULL restores the context's own stream). */
 mtr_status mtr_context_set_stream(mtr_context* ctx, void* cuda_stream);
 mtr_status mtr_context_synchronize(mtr_context* ctx);
-/* Number of libmtr kernel launches issued by this context so far. */
+/* Number of libmtr kernel launches issued by this process so far (graph
+ * replays count every kernel node). */
 mtr_status mtr_context_launch_count(const mtr_context* ctx, long long* out);
+
+/* Kernel classes for per-kernel timing. */
+#define MTR_KERNEL_WBP 0
+#define MTR_KERNEL_FORWARD 1
+#define MTR_KERNEL_RESIDUAL 2
+#define MTR_KERNEL_BACKPROJECT 3
+#define MTR_KERNEL_MACE 4
+#define MTR_KERNEL_OTHER 5
+#define MTR_KERNEL_CLASSES 6
+/* When enabled, every libmtr launch issued outside graph capture is
+ * bracketed by CUDA events on the context stream. */
+mtr_status mtr_context_set_profiling(mtr_context* ctx, int enable);
+/* Synchronises the stream and returns the accumulated launch count and
+ * device time (ms) of one kernel class since the last reset. */
+mtr_status mtr_context_profile(mtr_context* ctx, int kernel_class, long long* launches, double* total_ms);
+mtr_status mtr_context_profile_reset(mtr_context* ctx);
 
 /* ---- Entry points replacing FunctionOnGPU.cuh:41-44 -------------------- */
 

@@ -100,6 +100,11 @@ mtr_status mtr_context_destroy(mtr_context* ctx) {
   {
     DeviceGuard g(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    for (auto& r : ctx->prof_pending) {
+      cudaEventDestroy(r.a);
+      cudaEventDestroy(r.b);
+    }
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   }
   delete ctx;
@@ -124,6 +129,42 @@ mtr_status mtr_context_launch_count(const mtr_context* ctx, long long* out) {
   if (!out) return MTR_ERR_INVALID_ARGUMENT;
   (void)ctx;
   *out = g_launches.load();
+  return MTR_OK;
+}
+
+mtr_status mtr_context_set_profiling(mtr_context* ctx, int enable) {
+  if (!ctx) return MTR_ERR_INVALID_ARGUMENT;
+  ctx->profiling = enable != 0;
+  return MTR_OK;
+}
+
+mtr_status mtr_context_profile(mtr_context* ctx, int kernel_class, long long* launches, double* total_ms) {
+  if (!ctx || kernel_class < 0 || kernel_class >= MTR_KERNEL_CLASSES) return MTR_ERR_INVALID_ARGUMENT;
+  DeviceGuard g(ctx->device);
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_error(ctx, e, "cudaStreamSynchronize");
+  for (auto& r : ctx->prof_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+      ctx->prof_ms[r.kind] += ms;
+      ctx->prof_count[r.kind] += 1;
+    }
+    ctx->event_pool.push_back(r.a);
+    ctx->event_pool.push_back(r.b);
+  }
+  ctx->prof_pending.clear();
+  if (launches) *launches = ctx->prof_count[kernel_class];
+  if (total_ms) *total_ms = ctx->prof_ms[kernel_class];
+  return MTR_OK;
+}
+
+mtr_status mtr_context_profile_reset(mtr_context* ctx) {
+  if (!ctx) return MTR_ERR_INVALID_ARGUMENT;
+  mtr_context_profile(ctx, 0, nullptr, nullptr);
+  for (int i = 0; i < MTR_KERNEL_CLASSES; ++i) {
+    ctx->prof_count[i] = 0;
+    ctx->prof_ms[i] = 0.0;
+  }
   return MTR_OK;
 }
 

@@ -15,9 +15,48 @@ struct mtr_context {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   std::string last_error;
+  // Per-kernel-class event timing (mtr_context_set_profiling).
+  bool profiling = false;
+  struct ProfRec { int kind; cudaEvent_t a, b; };
+  std::vector<ProfRec> prof_pending;
+  std::vector<cudaEvent_t> event_pool;
+  long long prof_count[MTR_KERNEL_CLASSES] = {};
+  double prof_ms[MTR_KERNEL_CLASSES] = {};
+  cudaEvent_t take_event() {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+  }
 };
 
 namespace mtr {
+
+// Brackets the launches issued in its scope with events when profiling is on
+// and the stream is not being captured into a graph.
+struct ProfScope {
+  mtr_context* c;
+  int kind;
+  cudaEvent_t a = nullptr;
+  ProfScope(mtr_context* ctx, int k) : c(ctx), kind(k) {
+    if (!c || !c->profiling) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(c->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    a = c->take_event();
+    if (a) cudaEventRecord(a, c->stream);
+  }
+  ~ProfScope() {
+    if (!a) return;
+    cudaEvent_t b = c->take_event();
+    if (!b) return;
+    cudaEventRecord(b, c->stream);
+    c->prof_pending.push_back({kind, a, b});
+  }
+};
 
 // Process-wide count of libmtr kernel launches (graph replays add their node count).
 extern std::atomic<long long> g_launches;

@@ -77,6 +77,7 @@ mtr_status enqueue_geometry(mtr_recon* r) {
   const VolDev& v = r->vol;
   for (auto& a : r->ax) {
     MTR_CK(ctx, cudaMemsetAsync(a.cf.p, 0, (size_t)a.np * 4, ctx->stream));
+    ProfScope ps(ctx, MTR_KERNEL_OTHER);
     launch_forward<float>(a.dev(), v, nullptr, a.cf.as<float>(), v.Zs, v.Zs + v.NZ, ctx->stream);
     MTR_CK_LAUNCH(ctx, "forward row sums");
   }
@@ -87,6 +88,7 @@ mtr_status enqueue_forward(mtr_recon* r, AxisState& a) {
   mtr_context* ctx = r->ctx;
   const VolDev& v = r->vol;
   const int z0 = v.Zs, z1 = v.Zs + v.NZ;
+  ProfScope ps(ctx, MTR_KERNEL_FORWARD);
   switch (copy_kind_of(r->p.precision)) {
     case 1: launch_forward<__nv_bfloat16>(a.dev(), v, a.xcopy.as<__nv_bfloat16>(), a.s.as<float>(), z0, z1, ctx->stream); break;
     case 2: launch_forward<__half>(a.dev(), v, a.xcopy.as<__half>(), a.s.as<float>(), z0, z1, ctx->stream); break;
@@ -98,6 +100,7 @@ mtr_status enqueue_forward(mtr_recon* r, AxisState& a) {
 
 mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
   mtr_context* ctx = r->ctx;
+  ProfScope ps(ctx, MTR_KERNEL_RESIDUAL);
   if (mixed(r->p.precision))
     launch_residual<__half, __half>(a.np, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<__half>(), norm,
                                     ctx->stream);
@@ -113,6 +116,7 @@ mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const void* img_f32_
   const VolDev& v = r->vol;
   const int z0 = v.Zs, z1 = v.Zs + v.NZ;
   const int ck = copy_kind_of(r->p.precision);
+  ProfScope ps(ctx, mode == 0 ? MTR_KERNEL_WBP : MTR_KERNEL_BACKPROJECT);
   if (mixed(r->p.precision)) {
     const __half* img = mode == 0 ? a.b.as<__half>() : a.r.as<__half>();
     launch_backproject<__half>(a.dev(), v, img, mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(),
@@ -139,6 +143,7 @@ mtr_status enqueue_run(mtr_recon* r) {
   for (auto& a : r->ax) {
     mtr_status s = enqueue_bp(r, a, 0, nullptr);
     if (s != MTR_OK) return s;
+    ProfScope ps(ctx, MTR_KERNEL_OTHER);
     launch_axpy_acc(wavg, a.x.as<float>(), nv, ctx->stream);
     MTR_CK_LAUNCH(ctx, "initial model sum");
   }
@@ -147,6 +152,7 @@ mtr_status enqueue_run(mtr_recon* r) {
     MTR_CK(ctx, cudaMemcpyAsync(a.w.p, wavg, vbytes, cudaMemcpyDeviceToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDeviceToDevice, ctx->stream));
     if (ck) {
+      ProfScope ps(ctx, MTR_KERNEL_OTHER);
       launch_convert_copy(wavg, a.xcopy.p, ck, nv, ctx->stream);
       MTR_CK_LAUNCH(ctx, "volume copy");
     }
@@ -175,8 +181,11 @@ mtr_status enqueue_run(mtr_recon* r) {
         if (s != MTR_OK) return s;
       }
     }
-    launch_mace(K, ws.data(), xs.data(), wavg, nv, r->p.mace_step, xcs.data(), ck, dch ? dch + it : nullptr,
-                ctx->stream);
+    {
+      ProfScope ps(ctx, MTR_KERNEL_MACE);
+      launch_mace(K, ws.data(), xs.data(), wavg, nv, r->p.mace_step, xcs.data(), ck, dch ? dch + it : nullptr,
+                  ctx->stream);
+    }
     MTR_CK_LAUNCH(ctx, "mace");
   }
   return MTR_OK;

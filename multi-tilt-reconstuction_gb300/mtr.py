@@ -26,6 +26,7 @@ PREC_FP32, PREC_MIXED_BF16, PREC_MIXED_FP16 = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
 FLAG_RECORD_NORMS, FLAG_GRAPH = 1, 2
 MAX_AXES = 16
+KERNEL_CLASSES = ["wbp", "forward", "residual", "backproject", "mace", "other"]
 
 
 class MtrError(RuntimeError):
@@ -100,6 +101,9 @@ _SIGNATURES = {
     "mtr_context_set_stream": (C.c_int, [_P, _P]),
     "mtr_context_synchronize": (C.c_int, [_P]),
     "mtr_context_launch_count": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "mtr_context_set_profiling": (C.c_int, [_P, C.c_int]),
+    "mtr_context_profile": (C.c_int, [_P, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
+    "mtr_context_profile_reset": (C.c_int, [_P]),
     "mtr_wbp": (C.c_int, [_P, C.POINTER(AxisC), VolumeSize, C.c_int, C.c_int, _P]),
     "mtr_sirt": (C.c_int, [_P, C.POINTER(AxisC), VolumeSize, C.c_int, C.c_int, C.c_int, C.c_float, _P]),
     "mtr_initial_z": (C.c_int, [_P, VolumeSize, _P, _P, _P]),
@@ -222,6 +226,21 @@ class Context:
         n = C.c_longlong()
         self.check(self.lib.mtr_context_launch_count(self.h, C.byref(n)), "launch_count")
         return n.value
+
+    def set_profiling(self, on: bool) -> None:
+        self.check(self.lib.mtr_context_set_profiling(self.h, int(bool(on))), "set_profiling")
+
+    def profile(self) -> dict:
+        """{kernel class: (launches, total device ms)} since the last reset."""
+        out = {}
+        for k, name in enumerate(KERNEL_CLASSES):
+            n, ms = C.c_longlong(), C.c_double()
+            self.check(self.lib.mtr_context_profile(self.h, k, C.byref(n), C.byref(ms)), "profile")
+            out[name] = (n.value, ms.value)
+        return out
+
+    def profile_reset(self) -> None:
+        self.check(self.lib.mtr_context_profile_reset(self.h), "profile_reset")
 
     # --- reference-shaped entry points --------------------------------------------
     def wbp(self, axis: AxisData, vol: VolumeSize, z0: int | None = None, z1: int | None = None) -> np.ndarray:

@@ -171,3 +171,69 @@ def make_case(vol, n_px: int, tilts_deg, phis_deg, n_ellipsoids: int, noise: str
         data = proj.astype(np.float32)
         axes.append(axis_cls(xc, yc, data) if axis_cls else (xc, yc, data))
     return Case(vol, axes, ell, meta)
+
+
+def line_integrals_torch(ell: Ellipsoids, x_coef: np.ndarray, y_coef: np.ndarray, px: int, py: int,
+                         device="cuda", ell_chunk: int = 32) -> "object":
+    """Same analytic line integrals as line_integrals(), evaluated with torch
+    in FP64 on a CUDA device for the large benchmark sizes; returns a float32
+    CUDA tensor [A, py, px]."""
+    import torch
+
+    A = len(x_coef) // 4
+    out = torch.empty((A, py, px), dtype=torch.float32, device=device)
+    Q = torch.as_tensor(ell.Q, dtype=torch.float64, device=device)            # [n,3,3]
+    m = torch.as_tensor(ell.centre, dtype=torch.float64, device=device)       # [n,3]
+    rho = torch.as_tensor(ell.density, dtype=torch.float64, device=device)    # [n]
+    vv, uu = torch.meshgrid(torch.arange(py, dtype=torch.float64, device=device),
+                            torch.arange(px, dtype=torch.float64, device=device), indexing="ij")
+    for k in range(A):
+        xc, yc = x_coef[4 * k:4 * k + 4], y_coef[4 * k:4 * k + 4]
+        eu, ea = np.asarray(xc[1:]), np.asarray(yc[1:])
+        d = np.cross(eu, ea)
+        d /= np.linalg.norm(d)
+        Minv = torch.as_tensor(np.linalg.inv(np.stack([eu, ea, d])), dtype=torch.float64, device=device)
+        dd = torch.as_tensor(d, dtype=torch.float64, device=device)
+        p0 = (Minv[:, 0:1, None] * (uu + 1 - xc[0])[None] + Minv[:, 1:2, None] * (vv + 1 - yc[0])[None])  # [3,py,px]
+        p0 = p0.reshape(3, -1)
+        acc = torch.zeros(p0.shape[1], dtype=torch.float64, device=device)
+        Qd = torch.einsum("nij,j->ni", Q, dd)                                   # [n,3]
+        alpha = Qd @ dd                                                          # [n]
+        for s in range(0, len(ell.density), ell_chunk):
+            e = slice(s, s + ell_chunk)
+            r = p0[None] - m[e, :, None]                                         # [c,3,P]
+            beta = torch.einsum("ni,nip->np", Qd[e], r)
+            gamma = torch.einsum("nip,nij,njp->np", r, Q[e], r) - 1.0
+            disc = beta * beta - alpha[e, None] * gamma
+            chord = 2.0 * torch.sqrt(torch.clamp(disc, min=0.0)) / alpha[e, None]
+            acc += (rho[e, None] * chord).sum(0)
+        out[k] = acc.reshape(py, px).to(torch.float32)
+    return out
+
+
+def make_case_torch(vol, n_px: int, tilts_deg, phis_deg, n_ellipsoids: int, noise: str, level: float, seed: int,
+                    device="cuda") -> dict:
+    """Large-size counterpart of make_case: projections stay on the device
+    (float32 tensors); noise is drawn with a seeded torch generator."""
+    import torch
+
+    rng = np.random.default_rng(seed)
+    ell = random_ellipsoids(rng, n_ellipsoids, vol)
+    gen = torch.Generator(device=device)
+    gen.manual_seed(seed)
+    axes = []
+    meta = {"seed": seed, "noise": noise, "noise_params": []}
+    for phi in phis_deg:
+        xc, yc = axis_maps(n_px, n_px, tilts_deg, phi, vol)
+        proj = line_integrals_torch(ell, xc, yc, n_px, n_px, device)
+        if noise == "gaussian":
+            sigma = level * float(proj.max())
+            proj += sigma * torch.randn(proj.shape, generator=gen, device=device)
+            meta["noise_params"].append({"sigma": sigma})
+        elif noise == "poisson":
+            mu = 2.0 / max(float(proj.max()), 1e-12)
+            counts = torch.poisson(level * torch.exp(-mu * proj.double()), generator=gen)
+            proj = (-torch.log(torch.clamp(counts, min=1.0) / level) / mu).float()
+            meta["noise_params"].append({"mu": mu, "dose": level})
+        axes.append((xc, yc, proj.contiguous()))
+    return {"vol": vol, "axes": axes, "ellipsoids": ell, "meta": meta}
