@@ -182,9 +182,14 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     cfg = CONFIGS[args.config]
     torch.cuda.set_device(local_rank)
     device = f"cuda:{local_rank}"
-    stream = torch.cuda.current_stream()
+    # A dedicated stream: libmtr launches on it and the timing events are
+    # recorded on it (the legacy default stream's handle is 0, which the
+    # library would read as "use your own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     ctx = mtr.Context(local_rank)
     ctx.set_stream(stream.cuda_stream)
+    assert stream.cuda_stream != 0
     t0 = time.time()
     vol, axes, meta = make_inputs(cfg, device)
     gen_s = time.time() - t0

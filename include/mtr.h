@@ -180,6 +180,9 @@ mtr_status mtr_recon_upload(mtr_recon* r, int axis, const float* prj_data, int m
 mtr_status mtr_recon_run(mtr_recon* r);
 /* Copy w_avg out (host or device destination); synchronises for host. */
 mtr_status mtr_recon_download(mtr_recon* r, float* out, int mem_kind);
+/* Synchronises and reports MTR_ERR_TIMEOUT if a kernel of the last run gave
+ * up on a bounded wait (the host-buffer download performs this check). */
+mtr_status mtr_recon_check(mtr_recon* r);
 /* Copy the K per-axis MACE states w_k (K*X*Y*Z floats). */
 mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind);
 /* Squared residual norms, n_outer*K*n_inner doubles (MTR_FLAG_RECORD_NORMS). */

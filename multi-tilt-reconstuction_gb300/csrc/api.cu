@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -173,6 +174,11 @@ mtr_status mtr_context_profile_reset(mtr_context* ctx) {
 // ---------------------------------------------------------------------------
 // Validation helpers
 // ---------------------------------------------------------------------------
+
+bool mtr::tma_disabled() {
+  const char* e = std::getenv("MTR_DISABLE_TMA");
+  return e && e[0] == '1';
+}
 
 mtr_status mtr::check_volume(mtr_context* ctx, const mtr_volume_size& v) {
   if (v.X != v.Xend - v.Xstart || v.Y != v.Yend - v.Ystart || v.Z != v.Zend - v.Zstart)

@@ -1,0 +1,356 @@
+// Back-projection gather with TMA-staged projection windows (sm_103a).
+//
+// One CTA owns a brick of BX x BY x BZ voxels.  For every angle the brick's
+// footprint on the detector is a small window (<= 256 x 256 px); a producer
+// warp streams these windows into a ring of NST shared-memory stages with
+// 3-D tiled cp.async.bulk.tensor loads (one box per angle; pixels outside
+// the detector are zero-filled by the TMA unit, which is exactly the
+// reference's "drop taps outside the detector" for the numerator).  Eight
+// consumer warps gather the four bilinear taps of every voxel from shared
+// memory and accumulate over all angles in registers.
+//
+// Arithmetic per voxel and angle: one FFMA for the coordinate, FRND.FLOOR +
+// FADD for the fraction, an integer add to index the window (the float floor
+// is turned into an int by adding 1.5*2^23 and reading the bits, so no
+// float->int conversion runs in the loop), four LDS and six FFMA/FADD for the
+// interpolation.  When the y-map does not depend on Z (every synthetic and
+// single-axis TXBR geometry), the y-part is computed once per voxel column.
+//
+// All mbarrier waits are bounded; a wait that gives up sets *err and the CTA
+// drains its own in-flight copies (bounded) before returning.
+#include "mtr_internal.h"
+#include "tma.cuh"
+
+namespace mtr {
+namespace {
+
+constexpr int NST = 4;             // pipeline stages
+constexpr int kConsumerWarps = 8;  // 256 consumer threads
+constexpr int kThreads = (kConsumerWarps + 1) * 32;
+constexpr uint32_t kWaitIters = 1u << 24;
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: x + kMagic holds round(x) in its low bits
+constexpr int kMagicBits = 0x4B400000;
+
+struct WinConst {
+  float xf, a1, a2, a3;  // x map relative to the CTA base voxel (fractional base)
+  float yf, b1, b2, b3;
+  int lxm, lym;          // window-local integer base minus the magic bits
+  int ox, oy;            // window origin on the detector (ox aligned for TMA)
+};
+
+struct BpArgs {
+  AxisDev ax;
+  VolDev vol;
+  int z0, z1;
+  int WX, WY;       // window box (elements)
+  int align;        // TMA x alignment (elements)
+  int mode;         // 0 WBP, 1 SIRT
+  float step;
+  float* vol_out;
+  float* cbp;
+  void* vol_copy;
+  int copy_kind;
+  int* err;
+};
+
+template <typename PT> __device__ __forceinline__ float to_f(PT v);
+template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
+template <> __device__ __forceinline__ float to_f<__half>(__half v) { return __half2float(v); }
+
+__device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
+
+__device__ __forceinline__ int magic_int(float integral) { return __float_as_int(__fadd_rn(integral, kMagic)); }
+
+// LANE_Y: consecutive lanes walk Y (used when the detector x follows Y).
+template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
+__global__ void __launch_bounds__(kThreads)
+bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
+  constexpr int BX = LANE_Y ? kConsumerWarps : 32;
+  constexpr int BY = LANE_Y ? 32 : kConsumerWarps;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+  uint64_t* empty = full + NST;
+  WinConst* kc = reinterpret_cast<WinConst*>(smem + 128);
+  const int A = P.ax.A;
+  const size_t kc_bytes = ((size_t)A * sizeof(WinConst) + 127) & ~(size_t)127;
+  const int win_elems = P.WX * P.WY;
+  const size_t stage_bytes = (((size_t)win_elems * sizeof(PT)) + 127) & ~(size_t)127;
+  PT* win0 = reinterpret_cast<PT*>(smem + 128 + kc_bytes);
+
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int X0 = P.vol.Xs + blockIdx.x * BX;
+  const int Y0 = P.vol.Ys + blockIdx.y * BY;
+  const int Z0 = P.z0 + blockIdx.z * NZ;
+
+  if (tid == 0) {
+    for (int s = 0; s < NST; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kConsumerWarps);
+    }
+    mbar_fence_init();
+  }
+  // Per-angle constants: FP64 map at the base voxel, split into int + float.
+  for (int a = tid; a < A; a += kThreads) {
+    const double* cx = P.ax.xc + 4 * a;
+    const double* cy = P.ax.yc + 4 * a;
+    const double xb = cx[0] + cx[1] * X0 + cx[2] * Y0 + cx[3] * Z0 - 1.0;
+    const double yb = cy[0] + cy[1] * X0 + cy[2] * Y0 + cy[3] * Z0 - 1.0;
+    const double fxb = floor(fmin(fmax(xb, -1.0e9), 1.0e9)), fyb = floor(fmin(fmax(yb, -1.0e9), 1.0e9));
+    WinConst k;
+    k.xf = (float)(xb - fxb);
+    k.yf = (float)(yb - fyb);
+    k.a1 = (float)cx[1]; k.a2 = (float)cx[2]; k.a3 = (float)cx[3];
+    k.b1 = (float)cy[1]; k.b2 = (float)cy[2]; k.b3 = (float)cy[3];
+    const int xi = (int)fxb, yi = (int)fyb;
+    const float xmin = k.xf + fminf(0.f, k.a1 * (BX - 1)) + fminf(0.f, k.a2 * (BY - 1)) + fminf(0.f, k.a3 * (NZ - 1));
+    const float ymin = k.yf + fminf(0.f, k.b1 * (BX - 1)) + fminf(0.f, k.b2 * (BY - 1)) + fminf(0.f, k.b3 * (NZ - 1));
+    const int ox = floor_div(xi + (int)floorf(xmin) - 1, P.align) * P.align;
+    const int oy = yi + (int)floorf(ymin) - 1;
+    k.ox = ox;
+    k.oy = oy;
+    k.lxm = xi - ox - kMagicBits;
+    k.lym = yi - oy - kMagicBits;
+    kc[a] = k;
+  }
+  __syncthreads();
+
+  if (warp == kConsumerWarps) {
+    // ---------------- producer warp: one elected lane issues the TMA loads
+    if (lane == 0) {
+      prefetch_tensormap(&tmap);
+      const uint32_t bytes = (uint32_t)(win_elems * sizeof(PT));
+      int issued = 0;  // angles whose window load has been issued
+      for (int a = 0; a < A; ++a) {
+        const int s = a % NST;
+        const int n = a / NST;
+        if (n > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((n - 1) & 1), kWaitIters)) {
+          atomicExch(P.err, 2);
+          break;
+        }
+        PT* dst = reinterpret_cast<PT*>(reinterpret_cast<unsigned char*>(win0) + s * stage_bytes);
+        mbar_arrive_expect_tx(&full[s], bytes);
+        tma_load_3d(dst, &tmap, kc[a].ox, kc[a].oy, a, &full[s]);
+        issued = a + 1;
+      }
+      // Drain: the last load issued into each stage must land before exit
+      // (earlier ones into that stage completed before it could be reissued).
+      for (int s = 0; s < NST && s < issued; ++s) {
+        const int n_last = (issued - 1 - s) / NST;
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(n_last & 1), kWaitIters)) atomicExch(P.err, 3);
+      }
+    }
+    return;
+  }
+
+  // ---------------- consumer warps
+  const int tx = LANE_Y ? warp : lane;
+  const int ty = LANE_Y ? lane : warp;
+  const bool active = (X0 + tx < P.vol.Xs + P.vol.NX) && (Y0 + ty < P.vol.Ys + P.vol.NY);
+  const int WX = P.WX;
+  const unsigned lim_x = (unsigned)(WX - 1), lim_y = (unsigned)(P.WY - 1);
+  float s[NZ], c[NZ];
+#pragma unroll
+  for (int z = 0; z < NZ; ++z) { s[z] = 0.f; c[z] = 0.f; }
+  bool bad = false;
+
+  for (int a = 0; a < A; ++a) {
+    const int st = a % NST;
+    if (!mbar_wait_bounded(&full[st], (uint32_t)((a / NST) & 1), kWaitIters)) {
+      atomicExch(P.err, 4);
+      break;
+    }
+    const PT* w = reinterpret_cast<const PT*>(reinterpret_cast<const unsigned char*>(win0) + st * stage_bytes);
+    const WinConst k = kc[a];
+    const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
+    const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
+    if (active) {
+      // y part (per column when the map has no Z term)
+      float fy = 0.f, wy0 = 0.f, wy1 = 0.f, cy = 0.f;
+      int rowi = 0;
+      if (BZ0) {
+        const float fly = floorf(yr);
+        fy = yr - fly;
+        rowi = magic_int(fly) + k.lym;
+        if ((unsigned)rowi >= lim_y) bad = true;
+        wy0 = 1.f - fy;
+        wy1 = fy;
+        if (MODE == 0) {
+          const int iya = rowi + k.oy;
+          cy = ((unsigned)iya < (unsigned)P.ax.PY ? wy0 : 0.f) + ((unsigned)(iya + 1) < (unsigned)P.ax.PY ? wy1 : 0.f);
+        }
+      }
+#pragma unroll
+      for (int z = 0; z < NZ; ++z) {
+        if (!BZ0) {
+          const float y = fmaf(k.b3, (float)z, yr);
+          const float fly = floorf(y);
+          fy = y - fly;
+          rowi = magic_int(fly) + k.lym;
+          if ((unsigned)rowi >= lim_y) bad = true;
+          wy0 = 1.f - fy;
+          wy1 = fy;
+          if (MODE == 0) {
+            const int iya = rowi + k.oy;
+            cy = ((unsigned)iya < (unsigned)P.ax.PY ? wy0 : 0.f) +
+                 ((unsigned)(iya + 1) < (unsigned)P.ax.PY ? wy1 : 0.f);
+          }
+        }
+        const float x = fmaf(k.a3, (float)z, xr);
+        const float flx = floorf(x);
+        const float fx = x - flx;
+        const int ix = magic_int(flx) + k.lxm;
+        if ((unsigned)ix >= lim_x) bad = true;
+        const int i0 = bad ? 0 : ix + rowi * WX;  // never index outside the window
+        const float p00 = to_f(w[i0]), p10 = to_f(w[i0 + 1]);
+        const float p01 = to_f(w[i0 + WX]), p11 = to_f(w[i0 + WX + 1]);
+        const float r0 = fmaf(fx, p10 - p00, p00);
+        const float r1 = fmaf(fx, p11 - p01, p01);
+        s[z] = fmaf(wy0, r0, s[z]);
+        s[z] = fmaf(wy1, r1, s[z]);
+        if (MODE == 0) {
+          const int ixa = ix + k.ox;
+          const float cx = ((unsigned)ixa < (unsigned)P.ax.PX ? 1.f - fx : 0.f) +
+                           ((unsigned)(ixa + 1) < (unsigned)P.ax.PX ? fx : 0.f);
+          c[z] = fmaf(cx, cy, c[z]);
+        }
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);
+  }
+  if (bad) atomicExch(P.err, 5);
+  if (!active) return;
+
+  const long long sx = P.vol.NX, sxy = (long long)P.vol.NX * P.vol.NY;
+  const long long base = (long long)(X0 + tx - P.vol.Xs) + (long long)(Y0 + ty - P.vol.Ys) * sx;
+#pragma unroll
+  for (int z = 0; z < NZ; ++z) {
+    const int zz = Z0 + z;
+    if (zz >= P.z1) break;
+    const long long vi = base + (long long)(zz - P.z0) * sxy;
+    float out;
+    if (MODE == 0) {
+      out = (c[z] != 0.f) ? s[z] / c[z] : 0.f;
+      P.vol_out[vi] = out;
+      P.cbp[vi] = c[z];
+    } else {
+      const float cv = P.cbp[vi];
+      out = P.vol_out[vi];
+      if (cv != 0.f) {
+        out = fmaf(P.step, s[z] / cv, out);
+        P.vol_out[vi] = out;
+      }
+    }
+    if (P.copy_kind == 1) static_cast<__nv_bfloat16*>(P.vol_copy)[vi] = __float2bfloat16_rn(out);
+    else if (P.copy_kind == 2) static_cast<__half*>(P.vol_copy)[vi] = __float2half_rn(out);
+  }
+}
+
+template <typename PT, int MODE, bool LANE_Y, bool BZ0>
+cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cudaStream_t st) {
+  constexpr int NZ = 8;
+  auto kern = bp_tma_kernel<PT, MODE, LANE_Y, BZ0, NZ>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  const int BX = LANE_Y ? kConsumerWarps : 32, BY = LANE_Y ? 32 : kConsumerWarps;
+  const dim3 grid((P.vol.NX + BX - 1) / BX, (P.vol.NY + BY - 1) / BY, (P.z1 - P.z0 + NZ - 1) / NZ);
+  kern<<<grid, kThreads, smem, st>>>(map, P);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Window box for a brick of the given shape over all angles of an axis.
+BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half) {
+  BpPlan p;
+  p.align = half ? 8 : 4;
+  // Choose the lane axis so that consecutive lanes step along detector x.
+  double sx = 0, sy = 0;
+  bool bz0 = true;
+  for (int a = 0; a < A; ++a) {
+    sx += std::fabs(xc[4 * a + 1]) - std::fabs(yc[4 * a + 1]);
+    sy += std::fabs(xc[4 * a + 2]) - std::fabs(yc[4 * a + 2]);
+    if (yc[4 * a + 3] != 0.0) bz0 = false;
+  }
+  p.lane_y = sy > sx;
+  p.bz0 = bz0;
+  const int BX = p.lane_y ? kConsumerWarps : 32, BY = p.lane_y ? 32 : kConsumerWarps, BZ = 8;
+  double ex = 0, ey = 0;
+  for (int a = 0; a < A; ++a) {
+    ex = std::max(ex, std::fabs(xc[4 * a + 1]) * (BX - 1) + std::fabs(xc[4 * a + 2]) * (BY - 1) +
+                          std::fabs(xc[4 * a + 3]) * (BZ - 1));
+    ey = std::max(ey, std::fabs(yc[4 * a + 1]) * (BX - 1) + std::fabs(yc[4 * a + 2]) * (BY - 1) +
+                          std::fabs(yc[4 * a + 3]) * (BZ - 1));
+  }
+  // taps span [floor(min)-1, floor(max)+1], origin rounded down to the alignment
+  const int wx = (int)std::ceil(ex) + 4 + p.align;
+  p.WX = (wx + p.align - 1) / p.align * p.align;
+  p.WY = (int)std::ceil(ey) + 4;
+  p.ok = p.WX <= 256 && p.WY <= 256;
+  const size_t stage = (((size_t)p.WX * p.WY * (half ? 2 : 4)) + 127) & ~(size_t)127;
+  p.smem = 128 + ((((size_t)A * sizeof(WinConst)) + 127) & ~(size_t)127) + NST * stage;
+  if (p.smem > 227 * 1024) p.ok = false;
+  return p;
+}
+
+template <typename PT>
+cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, const AxisDev& ax, const VolDev& vol,
+                                   int mode, float step, float* vol_out, float* cbp, void* vol_copy, int copy_kind,
+                                   int z0, int z1, int* err, cudaStream_t st) {
+  BpArgs P{ax, vol, z0, z1, plan.WX, plan.WY, plan.align, mode, step, vol_out, cbp, vol_copy, copy_kind, err};
+#define MTR_BP_CASE(M, LY, BZ)                                                   \
+  if (mode == M && plan.lane_y == LY && plan.bz0 == BZ)                          \
+    return launch_one<PT, M, LY, BZ>(map, P, plan.smem, st);
+  MTR_BP_CASE(0, false, false) MTR_BP_CASE(0, false, true) MTR_BP_CASE(0, true, false) MTR_BP_CASE(0, true, true)
+  MTR_BP_CASE(1, false, false) MTR_BP_CASE(1, false, true) MTR_BP_CASE(1, true, false) MTR_BP_CASE(1, true, true)
+#undef MTR_BP_CASE
+  return cudaErrorInvalidValue;
+}
+
+template cudaError_t launch_backproject_tma<float>(const CUtensorMap&, const BpPlan&, const AxisDev&, const VolDev&,
+                                                   int, float, float*, float*, void*, int, int, int, int*,
+                                                   cudaStream_t);
+template cudaError_t launch_backproject_tma<__half>(const CUtensorMap&, const BpPlan&, const AxisDev&, const VolDev&,
+                                                    int, float, float*, float*, void*, int, int, int, int*,
+                                                    cudaStream_t);
+
+// ---- host: tensor-map encoding via the driver entry point -------------------
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+    else
+      cudaGetLastError();
+  }
+  return fn;
+}
+}  // namespace
+
+bool encode_tensor_map_3d(CUtensorMap* map, const void* base, bool half, int width, int pitch, int height, int depth,
+                          int bw, int bh) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const int es = half ? 2 : 4;
+  if (((uintptr_t)base & 15) || ((size_t)pitch * es) % 16 || (bw * es) % 16 || bw > 256 || bh > 256) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)width, (cuuint64_t)height, (cuuint64_t)depth};
+  cuuint64_t strides[2] = {(cuuint64_t)pitch * es, (cuuint64_t)pitch * es * height};
+  cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, half ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                  const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace mtr

@@ -30,7 +30,7 @@ mtr_status upload_axis(mtr_context* ctx, const mtr_axis& a, AxisUpload& u) {
   MTR_CK(ctx, cudaMemcpyAsync(u.xc.p, a.x_coef, sizeof(double) * 4 * a.prj.AngN, cudaMemcpyHostToDevice, ctx->stream));
   MTR_CK(ctx, cudaMemcpyAsync(u.yc.p, a.y_coef, sizeof(double) * 4 * a.prj.AngN, cudaMemcpyHostToDevice, ctx->stream));
   MTR_CK(ctx, cudaMemcpyAsync(u.b.p, a.prj_data, (size_t)np * 4, cudaMemcpyHostToDevice, ctx->stream));
-  u.dev = AxisDev{a.prj.X, a.prj.Y, a.prj.AngN, u.xc.as<double>(), u.yc.as<double>()};
+  u.dev = AxisDev{a.prj.X, a.prj.Y, a.prj.AngN, u.xc.as<double>(), u.yc.as<double>(), a.prj.X};
   return MTR_OK;
 }
 

@@ -1,6 +1,7 @@
 // Internal declarations shared by the CUDA translation units of libmtr.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
@@ -26,7 +27,12 @@ struct AxisDev {
   int PX, PY, A;
   const double* xc;  // [A*4]
   const double* yc;  // [A*4]
+  int pitch;         // row pitch of projection-space arrays, elements (>= PX)
 };
+
+// Row pitch used for device projection-space arrays: a multiple of 8
+// elements so that rows start on 16-byte boundaries for fp16 and fp32 (TMA).
+inline int projection_pitch(int px) { return (px + 7) / 8 * 8; }
 
 // Volume frame (absolute voxel coordinates, end-exclusive), identical to the
 // reference's VolumeSize (MrcFileIOBaseFunction.h:50-63).
@@ -57,6 +63,40 @@ void launch_forward(const AxisDev& ax, const VolDev& vol, const VT* x, float* s,
 template <typename BT, typename RT>
 void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, double* norm2,
                      cudaStream_t st);
+
+// ---- TMA-staged back-projection (bp_tma.cu) -------------------------------
+// Window geometry of one axis for the brick shape used by the TMA kernel.
+struct BpPlan {
+  bool ok = false;     // window fits the TMA box and shared-memory limits
+  bool lane_y = false; // lanes walk Y (detector x follows volume Y)
+  bool bz0 = false;    // y map independent of Z for every angle
+  int WX = 0, WY = 0;  // window box (elements)
+  int align = 4;       // TMA x alignment (elements)
+  size_t smem = 0;     // dynamic shared memory per CTA
+};
+BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half);
+template <typename PT>
+cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, const AxisDev& ax,
+                                   const VolDev& vol, int mode, float step, float* vol_out, float* cbp,
+                                   void* vol_copy, int copy_kind, int z0, int z1, int* err, cudaStream_t st);
+
+// 3-D tiled tensor map over [depth][height][pitch] fp32/fp16 elements with
+// logical width `width`, box (bw, bh, 1), zero fill (bp_tma.cu).
+bool encode_tensor_map_3d(CUtensorMap* map, const void* base, bool half, int width, int pitch, int height, int depth,
+                          int bw, int bh);
+
+// ---- windowed forward splat with TMA reduce (fwd_tma.cu) --------------------
+struct FwdPlan {
+  bool ok = false;
+  bool lane_y = false;
+  bool bz0 = false;
+  int WX = 0, WY = 0;
+  size_t smem = 0;
+};
+FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch);
+template <typename VT>
+cudaError_t launch_forward_tma(const CUtensorMap& smap, const FwdPlan& plan, const AxisDev& ax, const VolDev& vol,
+                               const VT* x, int z0, int z1, int* err, cudaStream_t st);
 
 // ---- elementwise / MACE (mace.cu) ----------------------------------------
 void launch_fill(float* p, long long n, float v, cudaStream_t st);

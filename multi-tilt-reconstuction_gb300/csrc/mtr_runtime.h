@@ -123,7 +123,15 @@ struct DevBuf {
 // Per-axis device state of a reconstruction.
 struct AxisState {
   int PX = 0, PY = 0, A = 0;
-  long long np = 0;       // A*PY*PX
+  int pitch = 0;          // row pitch of projection-space arrays (elements)
+  long long np = 0;       // A*PY*pitch
+  std::vector<double> hxc, hyc;  // host copies of the maps (kernel planning)
+  BpPlan plan;            // TMA back-projection window plan
+  CUtensorMap map_b{}, map_r{};  // tensor maps over b and r (valid when tma)
+  bool tma = false;
+  FwdPlan fplan;          // windowed forward splat plan
+  CUtensorMap map_s{}, map_cf{};  // tensor maps over s and cf (valid when ftma)
+  bool ftma = false;
   DevBuf xc, yc;          // [A*4] doubles
   DevBuf b;               // projections: float (FP32) or half (mixed)
   DevBuf s;               // forward accumulator, float
@@ -133,8 +141,12 @@ struct AxisState {
   DevBuf w;               // MACE state w_k (volume), float
   DevBuf x;               // SIRT iterate z_k -> v_k (volume), float
   DevBuf xcopy;           // bf16/f16 copy of x read by the forward pass (mixed)
-  AxisDev dev() const { return AxisDev{PX, PY, A, xc.as<double>(), yc.as<double>()}; }
+  AxisDev dev() const { return AxisDev{PX, PY, A, xc.as<double>(), yc.as<double>(), pitch}; }
 };
+
+// Disable the TMA kernels (MTR_DISABLE_TMA=1 in the environment) to run the
+// plain global-memory kernels instead; used to cross-check the two paths.
+bool tma_disabled();
 
 }  // namespace mtr
 
@@ -149,6 +161,7 @@ struct mtr_recon {
   mtr::DevBuf wavg;       // consensus volume, float
   mtr::DevBuf norms;      // n_outer*K*n_inner doubles
   mtr::DevBuf dchange;    // n_outer doubles
+  mtr::DevBuf err;        // device error flag written by bounded waits (int)
   long long bytes = 0;
   bool geometry_ready = false;  // cf and cbp computed
   cudaGraphExec_t graph = nullptr;

@@ -82,8 +82,8 @@ bp_gather_kernel(AxisDev ax, VolDev vol, const PT* __restrict__ img, float step,
 
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (X0 + tx >= vol.Xs + vol.NX || Y0 + ty >= vol.Ys + vol.NY) return;
-  const int PX = ax.PX, PY = ax.PY;
-  const long long plane = (long long)PX * PY;
+  const int PX = ax.PX, PY = ax.PY, RP = ax.pitch;
+  const long long plane = (long long)RP * PY;
 
   float s[kZR], c[kZR];
 #pragma unroll
@@ -104,8 +104,8 @@ bp_gather_kernel(AxisDev ax, VolDev vol, const PT* __restrict__ img, float step,
       const bool x0 = (unsigned)ix < (unsigned)PX, x1 = (unsigned)(ix + 1) < (unsigned)PX;
       const bool y0 = (unsigned)iy < (unsigned)PY, y1 = (unsigned)(iy + 1) < (unsigned)PY;
       if (MODE != 2) {
-        const PT* row0 = im + (long long)iy * PX + ix;
-        const PT* row1 = row0 + PX;
+        const PT* row0 = im + (long long)iy * RP + ix;
+        const PT* row1 = row0 + RP;
         const float p00 = (x0 && y0) ? ld_f(row0) : 0.f;
         const float p10 = (x1 && y0) ? ld_f(row0 + 1) : 0.f;
         const float p01 = (x0 && y1) ? ld_f(row1) : 0.f;
@@ -165,8 +165,8 @@ fwd_splat_kernel(AxisDev ax, VolDev vol, const VT* __restrict__ x, float* __rest
 
   const int tx = threadIdx.x, ty = threadIdx.y;
   if (X0 + tx >= vol.Xs + vol.NX || Y0 + ty >= vol.Ys + vol.NY) return;
-  const int PX = ax.PX, PY = ax.PY;
-  const long long plane = (long long)PX * PY;
+  const int PX = ax.PX, PY = ax.PY, RP = ax.pitch;
+  const long long plane = (long long)RP * PY;
 
   const long long sx = vol.NX, sxy = (long long)vol.NX * vol.NY;
   const long long base = (long long)(X0 + tx - vol.Xs) + (long long)(Y0 + ty - vol.Ys) * sx;
@@ -194,11 +194,11 @@ fwd_splat_kernel(AxisDev ax, VolDev vol, const VT* __restrict__ x, float* __rest
       const bool x0 = (unsigned)ix < (unsigned)PX, x1 = (unsigned)(ix + 1) < (unsigned)PX;
       const bool y0 = (unsigned)iy < (unsigned)PY, y1 = (unsigned)(iy + 1) < (unsigned)PY;
       const float g0 = (1.f - fy) * v[z], g1 = fy * v[z];
-      float* row0 = sp + (long long)iy * PX + ix;
+      float* row0 = sp + (long long)iy * RP + ix;
       if (x0 && y0) atomicAdd(row0, (1.f - fx) * g0);
       if (x1 && y0) atomicAdd(row0 + 1, fx * g0);
-      if (x0 && y1) atomicAdd(row0 + PX, (1.f - fx) * g1);
-      if (x1 && y1) atomicAdd(row0 + PX + 1, fx * g1);
+      if (x0 && y1) atomicAdd(row0 + RP, (1.f - fx) * g1);
+      if (x1 && y1) atomicAdd(row0 + RP + 1, fx * g1);
     }
   }
 }

@@ -54,17 +54,18 @@ mtr_status check_params(mtr_context* ctx, const mtr_params& p) {
   return MTR_OK;
 }
 
+// Projections [A][PY][PX] (caller layout) -> device [A][PY][pitch], padding zero.
 mtr_status upload_projections(mtr_recon* r, int k, const float* data, int mem_kind) {
   mtr_context* ctx = r->ctx;
   AxisState& a = r->ax[k];
   const size_t fbytes = (size_t)a.np * sizeof(float);
   const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-  if (!mixed(r->p.precision)) {
-    MTR_CK(ctx, cudaMemcpyAsync(a.b.p, data, fbytes, kind, ctx->stream));
-    return MTR_OK;
-  }
-  // Mixed: stage as float in the forward accumulator, convert to fp16.
-  MTR_CK(ctx, cudaMemcpyAsync(a.s.p, data, fbytes, kind, ctx->stream));
+  float* dst = mixed(r->p.precision) ? a.s.as<float>() : a.b.as<float>();
+  if (a.pitch != a.PX) MTR_CK(ctx, cudaMemsetAsync(dst, 0, fbytes, ctx->stream));
+  MTR_CK(ctx, cudaMemcpy2DAsync(dst, (size_t)a.pitch * 4, data, (size_t)a.PX * 4, (size_t)a.PX * 4,
+                                (size_t)a.PY * a.A, kind, ctx->stream));
+  if (!mixed(r->p.precision)) return MTR_OK;
+  // Mixed: staged as float in the forward accumulator, converted to fp16.
   launch_convert_copy(a.s.as<float>(), a.b.p, 2, a.np, ctx->stream);
   MTR_CK_LAUNCH(ctx, "convert projections");
   MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, fbytes, ctx->stream));
@@ -78,6 +79,13 @@ mtr_status enqueue_geometry(mtr_recon* r) {
   for (auto& a : r->ax) {
     MTR_CK(ctx, cudaMemsetAsync(a.cf.p, 0, (size_t)a.np * 4, ctx->stream));
     ProfScope ps(ctx, MTR_KERNEL_OTHER);
+    if (a.ftma) {
+      cudaError_t e = launch_forward_tma<float>(a.map_cf, a.fplan, a.dev(), v, nullptr, v.Zs, v.Zs + v.NZ,
+                                                r->err.as<int>(), ctx->stream);
+      g_launches.fetch_add(1);
+      if (e != cudaSuccess) return cuda_error(ctx, e, "forward row sums (tma)");
+      continue;
+    }
     launch_forward<float>(a.dev(), v, nullptr, a.cf.as<float>(), v.Zs, v.Zs + v.NZ, ctx->stream);
     MTR_CK_LAUNCH(ctx, "forward row sums");
   }
@@ -89,6 +97,20 @@ mtr_status enqueue_forward(mtr_recon* r, AxisState& a) {
   const VolDev& v = r->vol;
   const int z0 = v.Zs, z1 = v.Zs + v.NZ;
   ProfScope ps(ctx, MTR_KERNEL_FORWARD);
+  if (a.ftma) {
+    cudaError_t e;
+    switch (copy_kind_of(r->p.precision)) {
+      case 1: e = launch_forward_tma<__nv_bfloat16>(a.map_s, a.fplan, a.dev(), v, a.xcopy.as<__nv_bfloat16>(), z0, z1,
+                                                     r->err.as<int>(), ctx->stream); break;
+      case 2: e = launch_forward_tma<__half>(a.map_s, a.fplan, a.dev(), v, a.xcopy.as<__half>(), z0, z1,
+                                              r->err.as<int>(), ctx->stream); break;
+      default: e = launch_forward_tma<float>(a.map_s, a.fplan, a.dev(), v, a.x.as<float>(), z0, z1,
+                                              r->err.as<int>(), ctx->stream); break;
+    }
+    g_launches.fetch_add(1);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "forward splat (tma)");
+    return MTR_OK;
+  }
   switch (copy_kind_of(r->p.precision)) {
     case 1: launch_forward<__nv_bfloat16>(a.dev(), v, a.xcopy.as<__nv_bfloat16>(), a.s.as<float>(), z0, z1, ctx->stream); break;
     case 2: launch_forward<__half>(a.dev(), v, a.xcopy.as<__half>(), a.s.as<float>(), z0, z1, ctx->stream); break;
@@ -117,6 +139,19 @@ mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const void* img_f32_
   const int z0 = v.Zs, z1 = v.Zs + v.NZ;
   const int ck = copy_kind_of(r->p.precision);
   ProfScope ps(ctx, mode == 0 ? MTR_KERNEL_WBP : MTR_KERNEL_BACKPROJECT);
+  if (a.tma && !img_f32_or_null) {
+    const CUtensorMap& map = mode == 0 ? a.map_b : a.map_r;
+    cudaError_t e;
+    if (mixed(r->p.precision))
+      e = launch_backproject_tma<__half>(map, a.plan, a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
+                                         a.cbp.as<float>(), a.xcopy.p, ck, z0, z1, r->err.as<int>(), ctx->stream);
+    else
+      e = launch_backproject_tma<float>(map, a.plan, a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
+                                        a.cbp.as<float>(), nullptr, 0, z0, z1, r->err.as<int>(), ctx->stream);
+    g_launches.fetch_add(1);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "tma back-projection");
+    return MTR_OK;
+  }
   if (mixed(r->p.precision)) {
     const __half* img = mode == 0 ? a.b.as<__half>() : a.r.as<__half>();
     launch_backproject<__half>(a.dev(), v, img, mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(),
@@ -138,6 +173,7 @@ mtr_status enqueue_run(mtr_recon* r) {
   const size_t vbytes = (size_t)nv * 4;
   const int ck = copy_kind_of(r->p.precision);
   float* wavg = r->wavg.as<float>();
+  MTR_CK(ctx, cudaMemsetAsync(r->err.p, 0, sizeof(int), ctx->stream));
   // Initial model: sum over axes of each axis' WBP (MultiAxis.cpp:181-200).
   MTR_CK(ctx, cudaMemsetAsync(wavg, 0, vbytes, ctx->stream));
   for (auto& a : r->ax) {
@@ -201,7 +237,7 @@ mtr_status mtr_estimate_footprint(int n_axes, const mtr_projection_size* prjs, m
   const long long nv = (long long)vol.X * vol.Y * vol.Z;
   long long b = nv * 4;  // wavg
   for (int k = 0; k < n_axes; ++k) {
-    const long long np = (long long)prjs[k].X * prjs[k].Y * prjs[k].AngN;
+    const long long np = (long long)projection_pitch(prjs[k].X) * prjs[k].Y * prjs[k].AngN;
     b += axis_bytes(np, nv, precision) + 64LL * prjs[k].AngN;
   }
   *bytes = b;
@@ -236,13 +272,18 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   const bool mx = mixed(params->precision);
   const size_t vb = (size_t)r->nv * 4;
   MTR_CK(ctx, r->wavg.alloc(vb));
+  MTR_CK(ctx, r->err.alloc(sizeof(int)));
+  MTR_CK(ctx, cudaMemsetAsync(r->err.p, 0, sizeof(int), ctx->stream));
   r->bytes += vb;
   for (int k = 0; k < n_axes; ++k) {
     AxisState& a = r->ax[k];
     a.PX = axes[k].prj.X;
     a.PY = axes[k].prj.Y;
     a.A = axes[k].prj.AngN;
-    a.np = (long long)a.PX * a.PY * a.A;
+    a.pitch = projection_pitch(a.PX);
+    a.np = (long long)a.pitch * a.PY * a.A;
+    a.hxc.assign(axes[k].x_coef, axes[k].x_coef + 4 * a.A);
+    a.hyc.assign(axes[k].y_coef, axes[k].y_coef + 4 * a.A);
     const size_t pe = mx ? 2 : 4;
     MTR_CK(ctx, a.xc.alloc(sizeof(double) * 4 * a.A));
     MTR_CK(ctx, a.yc.alloc(sizeof(double) * 4 * a.A));
@@ -258,8 +299,20 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     MTR_CK(ctx, cudaMemcpyAsync(a.xc.p, axes[k].x_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemcpyAsync(a.yc.p, axes[k].y_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream));
+    MTR_CK(ctx, cudaMemsetAsync(a.r.p, 0, (size_t)a.np * pe, ctx->stream));
     s = upload_projections(r.get(), k, axes[k].prj_data, mem_kind);
     if (s != MTR_OK) return s;
+    // TMA kernels where the window geometry fits (else the plain kernels run).
+    if (!tma_disabled()) {
+      a.plan = plan_backproject(a.hxc, a.hyc, a.A, mx);
+      a.tma = a.plan.ok &&
+              encode_tensor_map_3d(&a.map_b, a.b.p, mx, a.PX, a.pitch, a.PY, a.A, a.plan.WX, a.plan.WY) &&
+              encode_tensor_map_3d(&a.map_r, a.r.p, mx, a.PX, a.pitch, a.PY, a.A, a.plan.WX, a.plan.WY);
+      a.fplan = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch);
+      a.ftma = a.fplan.ok &&
+               encode_tensor_map_3d(&a.map_s, a.s.p, false, a.pitch, a.pitch, a.PY, a.A, a.fplan.WX, a.fplan.WY) &&
+               encode_tensor_map_3d(&a.map_cf, a.cf.p, false, a.pitch, a.pitch, a.PY, a.A, a.fplan.WX, a.fplan.WY);
+    }
   }
   if (params->flags & MTR_FLAG_RECORD_NORMS) {
     const size_t n = (size_t)std::max(1, params->iter_times) * n_axes * std::max(1, params->sirt_inner);
@@ -318,7 +371,23 @@ mtr_status mtr_recon_download(mtr_recon* r, float* out, int mem_kind) {
   DeviceGuard g(ctx->device);
   const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
   MTR_CK(ctx, cudaMemcpyAsync(out, r->wavg.p, (size_t)r->nv * 4, kind, ctx->stream));
-  if (mem_kind != MTR_MEM_DEVICE) MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (mem_kind != MTR_MEM_DEVICE) {
+    MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+    return mtr_recon_check(r);
+  }
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_check(mtr_recon* r) {
+  if (!r) return MTR_ERR_INVALID_ARGUMENT;
+  mtr_context* ctx = r->ctx;
+  DeviceGuard g(ctx->device);
+  int flag = 0;
+  MTR_CK(ctx, cudaMemcpyAsync(&flag, r->err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  if (flag != 0)
+    return set_error(ctx, MTR_ERR_TIMEOUT,
+                     "a kernel gave up on a bounded wait or a window bound (code " + std::to_string(flag) + ")");
   return MTR_OK;
 }
 

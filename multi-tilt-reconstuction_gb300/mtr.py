@@ -115,6 +115,7 @@ _SIGNATURES = {
     "mtr_recon_run": (C.c_int, [_P]),
     "mtr_recon_download": (C.c_int, [_P, _P, C.c_int]),
     "mtr_recon_download_axes": (C.c_int, [_P, _P, C.c_int]),
+    "mtr_recon_check": (C.c_int, [_P]),
     "mtr_recon_norms": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong]),
     "mtr_recon_footprint": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "mtr_recon_destroy": (C.c_int, [_P]),

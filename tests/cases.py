@@ -21,6 +21,12 @@ CASES = {
     # four axes at 0/45/90/135 degrees with Poisson noise
     "four_axis": dict(vol=(0, 16, 0, 16, 0, 5), px=20, py=None, tilts=(-60, 61, 30), phis=(0.0, 45.0, 90.0, 135.0),
                       n_ell=5, noise=("poisson", 50.0), seed=14),
+    # detector wide enough for the windowed (TMA) forward splat; axes at 0 and 90 degrees
+    "mid": dict(vol=(-8, 56, 4, 52, 0, 20), px=72, py=None, tilts=(-60, 61, 10), phis=(0.0, 90.0), n_ell=6,
+                noise=("gaussian", 0.02), seed=16),
+    # oblique axes with a ragged volume (no dimension a multiple of the brick)
+    "mid_oblique": dict(vol=(0, 45, 0, 37, 0, 19), px=68, py=None, tilts=(-60, 61, 15), phis=(60.0, 135.0), n_ell=6,
+                        noise=("gaussian", 0.05), seed=17),
 }
 
 # Non-square detector: supported by the product and the oracle (the reference
@@ -39,3 +45,13 @@ def make(spec: dict) -> phantom.Case:
 
 def get(name: str) -> phantom.Case:
     return make(RECT if name == "rect" else CASES[name])
+
+
+def tilt_axis_in_z(case: phantom.Case, slope: float = 0.04) -> phantom.Case:
+    """Give every y-map a Z term (a tilt axis not parallel to the XY plane)."""
+    axes = []
+    for a in case.axes:
+        yc = a.y_coef.copy()
+        yc[3::4] += slope
+        axes.append(mtr.AxisData(a.x_coef, yc, a.data))
+    return phantom.Case(case.vol, axes, case.ellipsoids, case.meta)

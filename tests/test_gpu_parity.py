@@ -145,3 +145,33 @@ def test_reconstruct_matches_reference_kernels(ctx, name, no, ni, rho):
     got = ctx.reconstruct(c.axes, c.vol, p)
     want = oracle.ref_reconstruct(c.axes, c.vol, no, ni, 0.5, rho)
     assert rel_l2(got, want) < FP32_TOL
+
+
+# --- TMA-windowed kernels (detector wide enough for the windowed forward) -----------
+
+@pytest.mark.parametrize("name", ["mid", "mid_oblique"])
+@pytest.mark.parametrize("prec", [mtr.PREC_FP32, mtr.PREC_MIXED_BF16])
+def test_windowed_kernels_match_oracle(ctx, name, prec):
+    c = cases.get(name)
+    p = mtr.params(iter_times=2, sirt_inner=3, sirt_step=0.5, mace_step=0.8, precision=prec)
+    got = ctx.reconstruct(c.axes, c.vol, p)
+    mode = oracle.REF_FAITHFUL if prec == mtr.PREC_FP32 else oracle.FP64
+    want = oracle.reconstruct(mode, c.axes, c.vol, 2, 3, 0.5, 0.8)
+    assert rel_l2(got, want) < (FP32_TOL if prec == mtr.PREC_FP32 else MIXED_TOL)
+
+
+def test_windowed_kernels_z_dependent_y_map(ctx):
+    c = cases.tilt_axis_in_z(cases.get("mid"))
+    p = mtr.params(iter_times=1, sirt_inner=4, sirt_step=0.5, mace_step=0.7)
+    got = ctx.reconstruct(c.axes, c.vol, p)
+    want = oracle.reconstruct(oracle.REF_FAITHFUL, c.axes, c.vol, 1, 4, 0.5, 0.7)
+    assert rel_l2(got, want) < FP32_TOL
+
+
+def test_windowed_and_plain_kernels_agree(ctx, monkeypatch):
+    c = cases.get("mid_oblique")
+    p = mtr.params(iter_times=1, sirt_inner=3, sirt_step=0.5, mace_step=0.7)
+    tma = ctx.reconstruct(c.axes, c.vol, p)
+    monkeypatch.setenv("MTR_DISABLE_TMA", "1")
+    plain = ctx.reconstruct(c.axes, c.vol, p)
+    assert rel_l2(tma, plain) < 1e-5
