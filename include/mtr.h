@@ -165,6 +165,15 @@ mtr_status mtr_update_w(mtr_context* ctx, mtr_volume_size vol, const float* v, c
 mtr_status mtr_reconstruct(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
                            const mtr_params* params, float* out_volume);
 
+/* The same reconstruction with every quantity in FP64 on the GPU (affine
+ * map per voxel and angle, weights, sums, residual, MACE state), used as the
+ * error reference for the FP32 and mixed-precision paths.  No reference
+ * counterpart: the reference computes in FP64/float as the FP32 path does.
+ * out_volume: X*Y*Z doubles, host or device memory per mem_kind; axes'
+ * prj_data likewise. */
+mtr_status mtr_reconstruct_fp64(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
+                                const mtr_params* params, double* out_volume, int mem_kind);
+
 /* ---- Device-resident reconstruction object ------------------------------ */
 /* The same computation as mtr_reconstruct, split so that uploads, the
  * on-device run and the download can be issued (and timed) separately. */

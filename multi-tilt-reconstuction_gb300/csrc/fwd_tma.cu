@@ -5,16 +5,26 @@
 // with global float atomics (FunctionOnGPU.cu:27-52, 316-333): eight atomics
 // per voxel and angle, contending along every ray.  Here one CTA owns a
 // brick of BX x BY x NZ voxels, held in registers for the whole launch.  For
-// each angle it splats the brick into a private detector window in shared
-// memory (shared-memory atomics, no global traffic), then one thread flushes
-// the window to the ray-sum array with a single 3-D tiled
-// cp.reduce.async.bulk.tensor add (the L2 performs the reduction on whole
-// sectors).  Two window stages alternate so the flush of angle a overlaps
-// the splat of angle a+1.
+// each of its angles it splats the brick into a private detector window in
+// shared memory, then one thread flushes the window into the ray-sum array
+// with a single 3-D tiled cp.reduce.async.bulk.tensor add (the L2 reduces
+// whole sectors).  Two window stages alternate so the flush of one angle
+// overlaps the splat of the next.
+//
+// Window accumulation is fixed point: shared-memory float atomicAdd is not a
+// single native operation on this part, integer adds are.  Each CTA scales
+// its voxels by a power of two S with S * max|v| < 2^b, b <= 21, so every tap
+// weight*value rounds to an integer below 2^21 (rounded with the 1.5*2^23
+// trick, no float->int conversion) with an absolute error of at most
+// 2^-(b+1) * max|v|.  The host bounds the weight one pixel can receive from
+// one brick by 2^mass_shift (lattice points in the preimage of a 2x2-pixel
+// square, times the brick depth) and b = min(21, 30 - mass_shift) keeps every
+// window sum below 2^30.  Before the flush the window is converted back to
+// float and divided by S (exact: S is a power of two).
 //
 // Windows are clamped inside the detector (TMA reduces must not start at a
-// negative coordinate), so a window tap is on the detector iff it lies in the
-// window; taps off the detector are dropped as in the reference.
+// negative coordinate), so a tap is on the detector iff it lies in the valid
+// part of the window; taps off the detector are dropped as in the reference.
 #include "mtr_internal.h"
 #include "tma.cuh"
 
@@ -23,7 +33,8 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
-constexpr float kMagic = 12582912.0f;
+constexpr int kNZ = 16;
+constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
 struct FwdConst {
@@ -31,7 +42,7 @@ struct FwdConst {
   float yf, b1, b2, b3;
   int lxm, lym;  // window-local integer base minus the magic bits
   int ox, oy;    // window origin (clamped inside the detector, ox aligned)
-  int wlx;       // valid window columns (window part left of the detector's right edge)
+  int wlx;       // valid window columns (left of the detector's right edge)
   int pad[3];
 };
 
@@ -40,12 +51,17 @@ struct FwdArgs {
   VolDev vol;
   int z0, z1;
   int WX, WY;
+  int groups;      // angle groups (grid.z = z-blocks * groups)
+  int max_angles;  // angles per group (shared-memory constants sized for it)
+  int mass_shift;  // log2 bound of one pixel's total weight from one brick
   const void* x;   // volume (nullptr: ones)
   int* err;
 };
 
 __device__ __forceinline__ int magic_int(float integral) { return __float_as_int(__fadd_rn(integral, kMagic)); }
 __device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
+// round(w * v) for |w*v| < 2^22, as an integer, without a conversion instruction
+__device__ __forceinline__ int fixq(float w, float v) { return __float_as_int(fmaf(w, v, kMagic)) - kMagicBits; }
 
 template <typename VT> __device__ __forceinline__ float ldv(const void* p, long long i);
 template <> __device__ __forceinline__ float ldv<float>(const void* p, long long i) {
@@ -58,27 +74,33 @@ template <> __device__ __forceinline__ float ldv<__half>(const void* p, long lon
   return __half2float(__ldg(static_cast<const __half*>(p) + i));
 }
 
-template <typename VT, bool LANE_Y, bool BZ0, int NZ>
+template <typename VT, bool LANE_Y, bool BZ0>
 __global__ void __launch_bounds__(kThreads)
 fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
+  constexpr int NZ = kNZ;
   constexpr int BX = LANE_Y ? kWarps : 32;
   constexpr int BY = LANE_Y ? 32 : kWarps;
   extern __shared__ __align__(128) unsigned char smem[];
-  const int A = P.ax.A;
   FwdConst* kc = reinterpret_cast<FwdConst*>(smem);
-  const size_t kc_bytes = ((size_t)A * sizeof(FwdConst) + 127) & ~(size_t)127;
+  const size_t kc_bytes = ((size_t)P.max_angles * sizeof(FwdConst) + 127) & ~(size_t)127;
   const int WX = P.WX, WY = P.WY;
   const int win_elems = WX * WY;
   const size_t stage_bytes = ((size_t)win_elems * 4 + 127) & ~(size_t)127;
-  float* win0 = reinterpret_cast<float*>(smem + kc_bytes);
+  unsigned char* win0 = smem + kc_bytes + 128;
+  float* red = reinterpret_cast<float*>(smem + kc_bytes);  // 32 floats for the block max
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int zb = blockIdx.z / P.groups, g = blockIdx.z % P.groups;
+  const int A = P.ax.A;
+  const int a_begin = (int)((long long)A * g / P.groups), a_end = (int)((long long)A * (g + 1) / P.groups);
+  const int na = a_end - a_begin;
   const int X0 = P.vol.Xs + blockIdx.x * BX;
   const int Y0 = P.vol.Ys + blockIdx.y * BY;
-  const int Z0 = P.z0 + blockIdx.z * NZ;
+  const int Z0 = P.z0 + zb * NZ;
   const int PX = P.ax.PX, PY = P.ax.PY;
 
-  for (int a = tid; a < A; a += kThreads) {
+  for (int j = tid; j < na; j += kThreads) {
+    const int a = a_begin + j;
     const double* cx = P.ax.xc + 4 * a;
     const double* cy = P.ax.yc + 4 * a;
     const double xb = cx[0] + cx[1] * X0 + cx[2] * Y0 + cx[3] * Z0 - 1.0;
@@ -94,7 +116,7 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
     const float ymin = k.yf + fminf(0.f, k.b1 * (BX - 1)) + fminf(0.f, k.b2 * (BY - 1)) + fminf(0.f, k.b3 * (NZ - 1));
     int ox = floor_div(xi + (int)floorf(xmin) - 1, 4) * 4;
     int oy = yi + (int)floorf(ymin) - 1;
-    // clamp inside [0, pitch - WX] x [0, PY - WY]; the host guarantees both ranges exist
+    // clamp inside [0, pitch - WX] x [0, PY - WY]; the host checked both ranges exist
     ox = min(max(ox, 0), P.ax.pitch - WX);
     oy = min(max(oy, 0), PY - WY);
     k.ox = ox;
@@ -102,14 +124,15 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
     k.lxm = xi - ox - kMagicBits;
     k.lym = yi - oy - kMagicBits;
     k.wlx = min(WX, PX - ox);
-    kc[a] = k;
+    kc[j] = k;
   }
 
-  // own voxels, loaded once (coalesced along lanes)
+  // own voxels, loaded once (coalesced along lanes), and the brick's max |v|
   const int tx = LANE_Y ? warp : lane;
   const int ty = LANE_Y ? lane : warp;
   const bool active = (X0 + tx < P.vol.Xs + P.vol.NX) && (Y0 + ty < P.vol.Ys + P.vol.NY);
   float v[NZ];
+  float vmax = 0.f;
   {
     const long long sx = P.vol.NX, sxy = (long long)P.vol.NX * P.vol.NY;
     const long long base = (long long)(X0 + tx - P.vol.Xs) + (long long)(Y0 + ty - P.vol.Ys) * sx;
@@ -118,25 +141,40 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
       const int zz = Z0 + z;
       v[z] = 0.f;
       if (active && zz < P.z1) v[z] = P.x ? ldv<VT>(P.x, base + (long long)(zz - P.z0) * sxy) : 1.f;
+      vmax = fmaxf(vmax, fabsf(v[z]));
     }
   }
+  for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  if (lane == 0) red[warp] = vmax;
   __syncthreads();
+  vmax = red[0];
+  for (int w = 1; w < kWarps; ++w) vmax = fmaxf(vmax, red[w]);
+  // S = 2^(b-e) with vmax < 2^e: every |w*v*S| < 2^b <= 2^21 (magic rounding
+  // range) and a pixel's window sum < 2^(b + mass_shift) <= 2^30 (no overflow)
+  int e2 = 0;
+  if (vmax > 0.f && isfinite(vmax)) frexpf(vmax, &e2);
+  const int bits = min(21, 30 - P.mass_shift);
+  const int sexp = max(-120, min(120, bits - e2));
+  const float S = ldexpf(1.f, sexp), invS = ldexpf(1.f, -sexp);
+#pragma unroll
+  for (int z = 0; z < NZ; ++z) v[z] *= S;
   if (tid == 0) prefetch_tensormap(&smap);
 
-  bool bad = false;
-  for (int a = 0; a < A; ++a) {
-    const int st = a & 1;
-    float* w = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(win0) + st * stage_bytes);
-    // the bulk reduce that last read this stage (angle a-2) must be done reading
-    if (tid == 0 && a >= 2) bulk_wait_read<1>();
+  for (int j = 0; j < na; ++j) {
+    const int a = a_begin + j;
+    const int st = j & 1;
+    int* wi = reinterpret_cast<int*>(win0 + st * stage_bytes);
+    float* wf = reinterpret_cast<float*>(wi);
+    // the bulk reduce that last read this stage (two angles ago) must be done reading
+    if (tid == 0 && j >= 2) bulk_wait_read<1>();
     __syncthreads();
     for (int i = tid * 4; i < win_elems; i += kThreads * 4) {
-      if (i + 3 < win_elems) *reinterpret_cast<float4*>(w + i) = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (i + 3 < win_elems) *reinterpret_cast<int4*>(wi + i) = make_int4(0, 0, 0, 0);
       else
-        for (int j = i; j < win_elems; ++j) w[j] = 0.f;
+        for (int q = i; q < win_elems; ++q) wi[q] = 0;
     }
     __syncthreads();
-    const FwdConst k = kc[a];
+    const FwdConst k = kc[j];
     if (active) {
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
       const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
@@ -171,36 +209,46 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
         const bool x0ok = (unsigned)ix < (unsigned)k.wlx;
         const bool x1ok = (unsigned)(ix + 1) < (unsigned)k.wlx;
         const float g0 = wy0 * v[z], g1 = wy1 * v[z];
-        float* r0 = w + (rowi * WX + ix);
+        const float wx0 = 1.f - fx;
+        int* r0 = wi + (rowi * WX + ix);
         if (y0ok) {
-          if (x0ok) atomicAdd(r0, g0 - fx * g0);
-          if (x1ok) atomicAdd(r0 + 1, fx * g0);
+          if (x0ok) atomicAdd(r0, fixq(wx0, g0));
+          if (x1ok) atomicAdd(r0 + 1, fixq(fx, g0));
         }
         if (y1ok) {
-          if (x0ok) atomicAdd(r0 + WX, g1 - fx * g1);
-          if (x1ok) atomicAdd(r0 + WX + 1, fx * g1);
+          if (x0ok) atomicAdd(r0 + WX, fixq(wx0, g1));
+          if (x1ok) atomicAdd(r0 + WX + 1, fixq(fx, g1));
         }
       }
     }
+    __syncthreads();
+    // fixed point -> float (exact power-of-two scale), in place
+    for (int i = tid; i < win_elems; i += kThreads) wf[i] = (float)wi[i] * invS;
     fence_proxy_async_smem();
     __syncthreads();
     if (tid == 0) {
-      tma_reduce_add_3d(&smap, w, k.ox, k.oy, a);
+      tma_reduce_add_3d(&smap, wf, k.ox, k.oy, a);
       bulk_commit();
     }
   }
   if (tid == 0) bulk_wait_all();
-  if (bad && P.err) atomicExch(P.err, 6);
 }
 
 template <typename VT, bool LY, bool BZ>
-cudaError_t launch_one(const CUtensorMap& map, const FwdArgs& P, size_t smem, cudaStream_t st) {
-  constexpr int NZ = 16;
-  auto kern = fwd_tma_kernel<VT, LY, BZ, NZ>;
+cudaError_t launch_one(const CUtensorMap& map, FwdArgs P, size_t smem, int num_sms, cudaStream_t st) {
+  auto kern = fwd_tma_kernel<VT, LY, BZ>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int BX = LY ? kWarps : 32, BY = LY ? 32 : kWarps;
-  const dim3 grid((P.vol.NX + BX - 1) / BX, (P.vol.NY + BY - 1) / BY, (P.z1 - P.z0 + NZ - 1) / NZ);
+  const long long bricks = (long long)((P.vol.NX + BX - 1) / BX) * ((P.vol.NY + BY - 1) / BY) *
+                           ((P.z1 - P.z0 + kNZ - 1) / kNZ);
+  // split the angles over several CTAs when there are too few bricks to fill the GPU
+  const long long target = (long long)num_sms * 8;
+  int groups = (int)std::min<long long>((target + bricks - 1) / bricks, (long long)P.ax.A);
+  if (groups < 1) groups = 1;
+  P.groups = groups;
+  P.max_angles = (P.ax.A + groups - 1) / groups;
+  const dim3 grid((P.vol.NX + BX - 1) / BX, (P.vol.NY + BY - 1) / BY, ((P.z1 - P.z0 + kNZ - 1) / kNZ) * groups);
   kern<<<grid, kThreads, smem, st>>>(map, P);
   return cudaGetLastError();
 }
@@ -218,7 +266,7 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
   }
   p.lane_y = sy > sx;
   p.bz0 = bz0;
-  const int BX = p.lane_y ? kWarps : 32, BY = p.lane_y ? 32 : kWarps, BZ = 16;
+  const int BX = p.lane_y ? kWarps : 32, BY = p.lane_y ? 32 : kWarps, BZ = kNZ;
   double ex = 0, ey = 0;
   for (int a = 0; a < A; ++a) {
     ex = std::max(ex, std::fabs(xc[4 * a + 1]) * (BX - 1) + std::fabs(xc[4 * a + 2]) * (BY - 1) +
@@ -229,8 +277,24 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
   p.WX = ((int)std::ceil(ex) + 4 + 4 + 3) / 4 * 4;
   p.WY = (int)std::ceil(ey) + 4;
   const size_t stage = (((size_t)p.WX * p.WY * 4) + 127) & ~(size_t)127;
-  p.smem = ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 2 * stage;
-  p.ok = p.WX <= 256 && p.WY <= 256 && p.WX <= pitch && p.WY <= PY && p.smem <= 200 * 1024;
+  // constants for up to A angles (one group) + block-max scratch + 2 stages
+  p.smem = ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 128 + 2 * stage;
+  // Weight a pixel can receive from one brick: per Z plane at most the number
+  // of voxels whose taps reach it, i.e. lattice points in the preimage of a
+  // 2x2-pixel square under the in-plane map J (bounding box of J^-1 [-1,1]^2).
+  double count = 0;
+  bool singular = false;
+  for (int a = 0; a < A; ++a) {
+    const double j00 = xc[4 * a + 1], j01 = xc[4 * a + 2], j10 = yc[4 * a + 1], j11 = yc[4 * a + 2];
+    const double det = j00 * j11 - j01 * j10;
+    if (std::fabs(det) < 1e-3) { singular = true; break; }
+    const double wx = 2.0 * (std::fabs(j11) + std::fabs(j01)) / std::fabs(det);
+    const double wy = 2.0 * (std::fabs(j10) + std::fabs(j00)) / std::fabs(det);
+    count = std::max(count, (wx + 1.0) * (wy + 1.0));
+  }
+  p.mass_shift = (int)std::ceil(std::log2(std::max(1.0, count * BZ)));
+  p.ok = !singular && p.mass_shift <= 16 && p.WX <= 256 && p.WY <= 256 && p.WX <= pitch && p.WY <= PY &&
+         p.smem <= 200 * 1024;
   (void)PX;
   return p;
 }
@@ -238,11 +302,13 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
 template <typename VT>
 cudaError_t launch_forward_tma(const CUtensorMap& smap, const FwdPlan& plan, const AxisDev& ax, const VolDev& vol,
                                const VT* x, int z0, int z1, int* err, cudaStream_t st) {
-  FwdArgs P{ax, vol, z0, z1, plan.WX, plan.WY, x, err};
-  if (!plan.lane_y && plan.bz0) return launch_one<VT, false, true>(smap, P, plan.smem, st);
-  if (!plan.lane_y && !plan.bz0) return launch_one<VT, false, false>(smap, P, plan.smem, st);
-  if (plan.lane_y && plan.bz0) return launch_one<VT, true, true>(smap, P, plan.smem, st);
-  return launch_one<VT, true, false>(smap, P, plan.smem, st);
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  FwdArgs P{ax, vol, z0, z1, plan.WX, plan.WY, 1, ax.A, plan.mass_shift, x, err};
+  if (!plan.lane_y && plan.bz0) return launch_one<VT, false, true>(smap, P, plan.smem, sms, st);
+  if (!plan.lane_y && !plan.bz0) return launch_one<VT, false, false>(smap, P, plan.smem, sms, st);
+  if (plan.lane_y && plan.bz0) return launch_one<VT, true, true>(smap, P, plan.smem, sms, st);
+  return launch_one<VT, true, false>(smap, P, plan.smem, sms, st);
 }
 
 template cudaError_t launch_forward_tma<float>(const CUtensorMap&, const FwdPlan&, const AxisDev&, const VolDev&,

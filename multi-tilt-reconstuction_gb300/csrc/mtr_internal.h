@@ -91,6 +91,7 @@ struct FwdPlan {
   bool lane_y = false;
   bool bz0 = false;
   int WX = 0, WY = 0;
+  int mass_shift = 0;  // log2 bound of a pixel's weight from one brick
   size_t smem = 0;
 };
 FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch);

@@ -109,6 +109,7 @@ _SIGNATURES = {
     "mtr_initial_z": (C.c_int, [_P, VolumeSize, _P, _P, _P]),
     "mtr_update_w": (C.c_int, [_P, VolumeSize, _P, _P, _P, C.c_float]),
     "mtr_reconstruct": (C.c_int, [_P, C.c_int, C.POINTER(AxisC), VolumeSize, C.POINTER(Params), _P]),
+    "mtr_reconstruct_fp64": (C.c_int, [_P, C.c_int, C.POINTER(AxisC), VolumeSize, C.POINTER(Params), _P, C.c_int]),
     "mtr_recon_create": (C.c_int, [_P, C.c_int, C.POINTER(AxisC), VolumeSize, C.POINTER(Params), C.c_int,
                                    C.POINTER(_P)]),
     "mtr_recon_upload": (C.c_int, [_P, C.c_int, _P, C.c_int]),
@@ -278,6 +279,17 @@ class Context:
         arr = (AxisC * len(axes))(*[a.c_struct() for a in axes])
         out = np.empty(vol.shape, np.float32)
         self.check(self.lib.mtr_reconstruct(self.h, len(axes), arr, vol, C.byref(p), _ptr(out)), "mtr_reconstruct")
+        return out
+
+
+    def reconstruct_fp64(self, axes: Sequence[AxisData], vol: VolumeSize, p: Params, out=None,
+                         mem_kind=MEM_HOST):
+        """All-FP64 GPU reconstruction (error reference); returns float64 [Z, Y, X]."""
+        arr = (AxisC * len(axes))(*[a.c_struct() for a in axes])
+        if out is None:
+            out = np.empty(vol.shape, np.float64)
+        self.check(self.lib.mtr_reconstruct_fp64(self.h, len(axes), arr, vol, C.byref(p), _ptr(out), mem_kind),
+                   "mtr_reconstruct_fp64")
         return out
 
 
