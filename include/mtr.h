@@ -147,6 +147,25 @@ mtr_status mtr_wbp(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol, 
 mtr_status mtr_sirt(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol, int slice_start,
                     int slice_end, int n_inner, float sirt_step, float* slab_inout);
 
+/* No counterpart in the reference.  The computation of mtr_sirt for callers
+ * that cannot allocate device memory where they call it (cudaMalloc and
+ * cudaFree synchronise the device and can fail, which a pipeline stage that
+ * must not stall, or a program whose device memory belongs to another
+ * allocator, cannot accept).  Inputs and outputs are device pointers owned by
+ * the caller: x_coef_dev / y_coef_dev (4*AngN doubles each), prj_dev
+ * (AngN*Y*X floats, x fastest) and slab_dev (X*Y*(slice_end-slice_start)
+ * floats, updated in place), enqueued on the context stream.  The working
+ * arrays live in one fixed device array of MTR_NOALLOC_SCRATCH_FLOATS floats
+ * (32 MiB) compiled into the library and held by every GPU that loads it:
+ * 3*AngN*Y*X + X*Y*(slice_end-slice_start) must not exceed it, else
+ * MTR_ERR_CAPACITY.  All calls share that array: calls that overlap on the
+ * GPU race, so issue them in order on one stream.  The first call on a device
+ * looks up the array's device address; make it before any stream capture. */
+#define MTR_NOALLOC_SCRATCH_FLOATS (8 * 1024 * 1024)
+mtr_status mtr_sirt_noalloc(mtr_context* ctx, mtr_projection_size prj, const double* x_coef_dev,
+                            const double* y_coef_dev, const float* prj_dev, mtr_volume_size vol, int slice_start,
+                            int slice_end, int n_inner, float sirt_step, float* slab_dev);
+
 /* Replaces initialZdata (FunctionOnGPU.cuh:43, FunctionOnGPU.cu:291-313):
  * z = 2*w_avg - w over the whole volume (host buffers). */
 mtr_status mtr_initial_z(mtr_context* ctx, mtr_volume_size vol, const float* w, const float* w_avg,

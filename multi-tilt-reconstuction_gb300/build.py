@@ -27,7 +27,8 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-
                      "--expt-relaxed-constexpr", "-I", str(INCLUDE)]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", "-I", str(INCLUDE)]
 
-CU_SOURCES = ["projector.cu", "bp_tma.cu", "fwd_tma.cu", "mace.cu", "api.cu", "recon.cu", "entry.cu", "ref64.cu"]
+CU_SOURCES = ["projector.cu", "bp_tma.cu", "fwd_tma.cu", "mace.cu", "api.cu", "recon.cu", "entry.cu", "ref64.cu",
+              "noalloc.cu"]
 CXX_SOURCES = ["mrc_io.cpp", "options.cpp"]
 
 

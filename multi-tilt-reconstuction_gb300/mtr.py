@@ -106,6 +106,8 @@ _SIGNATURES = {
     "mtr_context_profile_reset": (C.c_int, [_P]),
     "mtr_wbp": (C.c_int, [_P, C.POINTER(AxisC), VolumeSize, C.c_int, C.c_int, _P]),
     "mtr_sirt": (C.c_int, [_P, C.POINTER(AxisC), VolumeSize, C.c_int, C.c_int, C.c_int, C.c_float, _P]),
+    "mtr_sirt_noalloc": (C.c_int, [_P, ProjectionSize, _P, _P, _P, VolumeSize, C.c_int, C.c_int, C.c_int, C.c_float,
+                                   _P]),
     "mtr_initial_z": (C.c_int, [_P, VolumeSize, _P, _P, _P]),
     "mtr_update_w": (C.c_int, [_P, VolumeSize, _P, _P, _P, C.c_float]),
     "mtr_reconstruct": (C.c_int, [_P, C.c_int, C.POINTER(AxisC), VolumeSize, C.POINTER(Params), _P]),
