@@ -58,6 +58,25 @@ def peaks() -> tuple[dict, str]:
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+def reduce_max(x: float, device=None) -> float:
+    """Max of x over all ranks of the default process group (identity when not
+    distributed).  Works on NCCL (CUDA tensor) and gloo (CPU tensor)."""
+    import torch
+
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return x
+    dev = device if torch.distributed.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(units_per_rank: float, world: int, max_ms_per_step: float) -> float:
+    """Whole-job throughput of N independent replicas: every rank's units over
+    the slowest rank's time per step."""
+    return units_per_rank * world / (max_ms_per_step * 1e-3)
+
+
 def voxel_updates(cfg: dict) -> int:
     v = cfg["vol"]
     V = (v[1] - v[0]) * (v[3] - v[2]) * (v[5] - v[4])
@@ -159,9 +178,9 @@ def algorithmic_bytes(kind: str, cfg: dict, prec: int) -> tuple[float, str]:
     P = cfg["px"] * cfg["px"] * n_angles(cfg)
     pe = 2 if prec != mtr.PREC_FP32 else 4
     if kind == "backproject":
-        # read r (P), read+write the FP32 iterate, read the weight sums (+ write the bf16 copy when mixed)
-        b = P * pe + V * 12 + (V * 2 if prec != mtr.PREC_FP32 else 0)
-        return b, f"P*{pe} (residual) + V*12 (iterate r/w, weight sums){' + V*2 (bf16 copy)' if pe == 2 else ''}"
+        # read r (FP32, P), read+write the FP32 iterate, read the weight sums (+ write the bf16 copy when mixed)
+        b = P * 4 + V * 12 + (V * 2 if prec != mtr.PREC_FP32 else 0)
+        return b, f"P*4 (residual) + V*12 (iterate r/w, weight sums){' + V*2 (bf16 copy)' if pe == 2 else ''}"
     if kind == "forward":
         vb = 2 if prec != mtr.PREC_FP32 else 4
         return P * 4 + V * vb, f"V*{vb} (volume read) + P*4 (ray-sum write)"
@@ -198,6 +217,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     mk = lambda pr: mtr.params(iter_times=no, sirt_inner=ni, sirt_step=cfg["sirt_step"], mace_step=cfg["mace_step"],
                                precision=pr)
     rec = mtr.Recon(ctx, axes, vol, mk(prec), mem_kind=mtr.MEM_DEVICE)
+    tiles = rec.describe()
     ref32 = mtr.Recon(ctx, axes, vol, mk(mtr.PREC_FP32), mem_kind=mtr.MEM_DEVICE) if prec != mtr.PREC_FP32 else rec
 
     def barrier():
@@ -205,11 +225,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
             torch.distributed.barrier()
 
     def max_over_ranks(x: float) -> float:
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=device)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(x, device)
 
     # warm-up
     for _ in range(args.warmup):
@@ -267,7 +283,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     e2e_ms = max_over_ranks(statistics.mean(arr_ms))
 
     vu = voxel_updates(cfg)
-    res = {"ms": ms, "ms32": ms32, "e2e_ms": e2e_ms, "h2d": h2d, "d2h": vol.X * vol.Y * vol.Z * 4, "clk": clk,
+    res = {"tiles": tiles, "ms": ms, "ms32": ms32, "e2e_ms": e2e_ms, "h2d": h2d, "d2h": vol.X * vol.Y * vol.Z * 4, "clk": clk,
            "prof": prof, "launches": launches, "gen_s": gen_s, "meta": meta, "vu": vu,
            "mixed_vs_fp32": float(np.linalg.norm(out_mixed.astype(np.float64) - out_fp32) /
                                   max(np.linalg.norm(out_fp32.astype(np.float64)), 1e-30)),
@@ -277,6 +293,94 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         ref32.close()
     ctx.close()
     return res
+
+
+C4 = dict(workload="64 seeded tilt series, detector and volume lateral size U{128..1024} px, tilts U{41..121} "
+                   "over +-60 deg, axes U{1..4} (in-plane angles k*180/K), depth U{32..256}, 8 ellipsoids each, "
+                   "Gaussian noise 0.02; WBP init, 1 MACE x 3 SIRT, lambda 0.5, rho 0.7",
+          n=64, seed=1004, n_ell=8, n_outer=1, n_inner=3)
+
+
+def make_batch_instances(device: str):
+    """The 64 uneven instances (host float32 projections; generated on the GPU)."""
+    import torch
+
+    import mtr
+    import phantom
+
+    rng = np.random.default_rng(C4["seed"])
+    inst = []
+    for i in range(C4["n"]):
+        px = int(rng.integers(128, 1025))
+        A = int(rng.integers(41, 122))
+        K = int(rng.integers(1, 5))
+        Z = int(rng.integers(32, 257))
+        vol = mtr.VolumeSize.make(0, px, 0, px, 0, Z)
+        tilts = np.linspace(-60.0, 60.0, A)
+        phis = [k * 180.0 / K for k in range(K)]
+        case = phantom.make_case_torch(vol, px, tilts, phis, C4["n_ell"], "gaussian", 0.02, C4["seed"] * 100 + i,
+                                       device=device)
+        axes = [mtr.AxisData(xc, yc, d.cpu().numpy()) for (xc, yc, d) in case["axes"]]
+        del case
+        torch.cuda.empty_cache()
+        inst.append((axes, vol))
+    return inst
+
+
+def run_batch_bench(args) -> dict:
+    """Config 4: all instances in one batch (one persistent launch per SIRT phase,
+    CUDA graph, BF16 storage) against looping the plain FP32 path over them."""
+    import torch
+
+    import mtr
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = mtr.Context(0)
+    ctx.set_stream(stream.cuda_stream)
+    t0 = time.time()
+    inst = make_batch_instances("cuda:0")
+    gen_s = time.time() - t0
+    prec = {"bf16": mtr.PREC_MIXED_BF16, "fp16": mtr.PREC_MIXED_FP16, "fp32": mtr.PREC_FP32}[args.precision]
+    p = mtr.params(iter_times=C4["n_outer"], sirt_inner=C4["n_inner"], sirt_step=0.5, mace_step=0.7, precision=prec,
+                   flags=mtr.FLAG_GRAPH)
+    t0 = time.time()
+    batch = mtr.Batch(ctx, inst, p)
+    create_s = time.time() - t0
+    info = batch.info()
+    for _ in range(max(1, args.warmup)):
+        batch.run()
+    launches0 = ctx.launch_count()
+    ms = time_steps(torch, stream, batch, args.steps)
+    launches = (ctx.launch_count() - launches0) // max(1, args.steps)
+    batched = [batch.download(i) for i in range(len(inst))]
+    batch.close()
+    # plain FP32 path looped over the instances (device-resident inputs, run only timed)
+    pf = mtr.params(iter_times=C4["n_outer"], sirt_inner=C4["n_inner"], sirt_step=0.5, mace_step=0.7)
+    loop_ms, errs = 0.0, []
+    for i, (axes, vol) in enumerate(inst):
+        r = mtr.Recon(ctx, axes, vol, pf)
+        r.run()  # warm-up (module load, first-touch)
+        loop_ms += time_steps(torch, stream, r, 1)
+        ref = r.download()
+        r.close()
+        errs.append(float(np.linalg.norm(batched[i] - ref) / max(np.linalg.norm(ref), 1e-30)))
+    vu = info["voxel_updates"]
+    sizes = [vol.X for _, vol in inst]
+    return {"metric": METRIC, "value": vu / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": C4["workload"], "precision": args.precision, "instances": len(inst),
+                       "axes_total": sum(len(a) for a, _ in inst), "voxel_updates_per_step": vu,
+                       "device_bytes": info["bytes"], "work_items": info["items"],
+                       "lateral_px": [min(sizes), max(sizes)], "seed": C4["seed"],
+                       "l2": "inputs larger than L2", "generation_s": round(gen_s, 1),
+                       "create_and_tune_s": round(create_s, 1)},
+            "fp32_loop": {"value": vu / (loop_ms * 1e-3), "ms_per_step": loop_ms,
+                          "batched_over_loop": loop_ms / ms,
+                          "rel_l2_batched_vs_fp32_max": max(errs), "rel_l2_batched_vs_fp32_median": float(np.median(errs))},
+            "gpu_launches": launches, "e2e": None}
 
 
 def cpu_baseline(cfg: dict, vol, axes_host, budget_s: float = 20.0) -> dict:
@@ -342,7 +446,7 @@ def main() -> int:
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS))
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c4"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
@@ -360,6 +464,11 @@ def main() -> int:
         return 0
 
     import __graft_entry__
+
+    if args.config == "c4":
+        __graft_entry__.build()
+        print(json.dumps(run_batch_bench(args)), flush=True)
+        return 0
 
     if rank == 0 or world == 1:
         __graft_entry__.build()
@@ -389,16 +498,19 @@ def main() -> int:
                 "avg_launch_ms": per_launch_ms, "launches": n_l,
                 "kernel_share": {k: prof[k][1] / max(sum(x[1] for x in prof.values()), 1e-9) for k in prof}}
         vu = r["vu"] * world
-        value = vu / (r["ms"] * 1e-3)
+        value = replica_value(r["vu"], world, r["ms"])
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": cfg["workload"], "precision": args.precision,
-                       "storage": "bf16 volume copy, fp16 projections/residuals" if args.precision != "fp32"
+                       "storage": f"{args.precision} volume copy for the forward pass, fp16 projections, "
+                                  "fp32 iterate/residual/MACE state" if args.precision != "fp32"
                        else "fp32", "voxel_updates_per_step": r["vu"], "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (each volume array 134 MB, projections 64 MB per axis)",
-                       "seed": cfg["seed"]},
+                       "seed": cfg["seed"],
+                       "tiles": [{"bp_depth": t["back_projection"]["depth"], "fwd_depth": t["forward"]["depth"],
+                                  "tma": t["back_projection"]["tma"] and t["forward"]["tma"]} for t in r["tiles"]]},
             "fp32": {"value": vu / (r["ms32"] * 1e-3), "ms_per_step": r["ms32"],
                      "mixed_over_fp32": r["ms32"] / r["ms"]},
             "error": {"mixed_vs_fp32_rel_l2": r["mixed_vs_fp32"]},

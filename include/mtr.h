@@ -41,11 +41,11 @@ typedef enum mtr_status {
   MTR_ERR_CAPACITY = 10
 } mtr_status;
 
-/* Storage precision.  FP32: everything float.  MIXED_*: projections and
- * residuals stored FP16, the volume copy read by the forward projector
- * stored BF16 (or FP16); interpolation and accumulation in FP32; residual
- * norms and the MACE consensus sum in FP64; the SIRT iterate and the MACE
- * state stay FP32. */
+/* Storage precision.  FP32: everything float.  MIXED_*: projections stored
+ * FP16, the volume copy read by the forward projector stored BF16 (or FP16);
+ * interpolation and accumulation in FP32; residual norms and the MACE
+ * consensus sum in FP64; the SIRT iterate, the residual and the MACE state
+ * stay FP32. */
 typedef enum mtr_precision {
   MTR_PREC_FP32 = 0,
   MTR_PREC_MIXED_BF16 = 1,
@@ -217,10 +217,40 @@ mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind);
 mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n);
 /* Device bytes held by the object. */
 mtr_status mtr_recon_footprint(const mtr_recon* r, long long* bytes);
+/* JSON description of the kernels and tile shapes chosen per axis (TMA
+ * windows, brick depths picked by the autotuner); NUL-terminated, truncated
+ * to cap bytes. */
+mtr_status mtr_recon_describe(const mtr_recon* r, char* buf, int cap);
 mtr_status mtr_recon_destroy(mtr_recon* r);
 /* Device bytes an object with these shapes would hold (admission control). */
 mtr_status mtr_estimate_footprint(int n_axes, const mtr_projection_size* prjs, mtr_volume_size vol,
                                   int precision, long long* bytes);
+
+/* ---- Batched reconstruction of many tilt series ------------------------- */
+/* No counterpart in the reference (it reconstructs one series per MPI job).
+ * Every instance gets its own device-resident reconstruction; the SIRT
+ * phases of all instances run as one persistent launch per phase over a
+ * cost-ordered work list of (instance, axis, brick) items, and the whole
+ * schedule is captured once into a CUDA graph when params->flags has
+ * MTR_FLAG_GRAPH.  All instances share params (iterations, steps, precision);
+ * residual norms are not recorded in batch mode. */
+typedef struct mtr_instance {
+  int n_axes;
+  const mtr_axis* axes;
+  mtr_volume_size vol;
+} mtr_instance;
+typedef struct mtr_batch mtr_batch;
+mtr_status mtr_batch_create(mtr_context* ctx, int n, const mtr_instance* instances, const mtr_params* params,
+                            int mem_kind, mtr_batch** out);
+/* WBP init + MACE loop of every instance (asynchronous on the context stream). */
+mtr_status mtr_batch_run(mtr_batch* b);
+/* Consensus volume of instance i (host: synchronises and checks the error flag). */
+mtr_status mtr_batch_download(mtr_batch* b, int i, float* out, int mem_kind);
+/* Voxel-updates per run, device bytes held, and work items per phase
+ * (forward, residual, back-projection, MACE, axes on fallback kernels). */
+mtr_status mtr_batch_info(const mtr_batch* b, long long* voxel_updates_per_run, long long* device_bytes,
+                          long long* work_items5);
+mtr_status mtr_batch_destroy(mtr_batch* b);
 
 /* ---- MRC / TXBR / options (the reference's file I/O boundary) ----------- */
 

@@ -18,6 +18,8 @@
 //
 // All mbarrier waits are bounded; a wait that gives up sets *err and the CTA
 // drains its own in-flight copies (bounded) before returning.
+#include <type_traits>
+
 #include "mtr_internal.h"
 #include "tma.cuh"
 
@@ -61,13 +63,14 @@ __device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b
 
 __device__ __forceinline__ int magic_int(float integral) { return __float_as_int(__fadd_rn(integral, kMagic)); }
 
-// LANE_Y: consecutive lanes walk Y (used when the detector x follows Y).
+// One brick (bx, by, bz) of one axis.  LANE_Y: consecutive lanes walk Y (used
+// when the detector x follows Y).  `smem` is the CTA's dynamic shared memory;
+// `reinit` re-initialises the mbarriers of a CTA that already ran a brick.
 template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
-__global__ void __launch_bounds__(kThreads)
-bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
+__device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& P, int bx, int by, int bz,
+                                         unsigned char* smem, bool reinit) {
   constexpr int BX = LANE_Y ? kConsumerWarps : 32;
   constexpr int BY = LANE_Y ? 32 : kConsumerWarps;
-  extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + NST;
   WinConst* kc = reinterpret_cast<WinConst*>(smem + 128);
@@ -79,12 +82,16 @@ bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
-  const int X0 = P.vol.Xs + blockIdx.x * BX;
-  const int Y0 = P.vol.Ys + blockIdx.y * BY;
-  const int Z0 = P.z0 + blockIdx.z * NZ;
+  const int X0 = P.vol.Xs + bx * BX;
+  const int Y0 = P.vol.Ys + by * BY;
+  const int Z0 = P.z0 + bz * NZ;
 
   if (tid == 0) {
     for (int s = 0; s < NST; ++s) {
+      if (reinit) {
+        mbar_inval(&full[s]);
+        mbar_inval(&empty[s]);
+      }
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], kConsumerWarps);
     }
@@ -118,7 +125,7 @@ bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   if (warp == kConsumerWarps) {
     // ---------------- producer warp: one elected lane issues the TMA loads
     if (lane == 0) {
-      prefetch_tensormap(&tmap);
+      prefetch_tensormap(tmap);
       const uint32_t bytes = (uint32_t)(win_elems * sizeof(PT));
       int issued = 0;  // angles whose window load has been issued
       for (int a = 0; a < A; ++a) {
@@ -130,7 +137,7 @@ bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
         }
         PT* dst = reinterpret_cast<PT*>(reinterpret_cast<unsigned char*>(win0) + s * stage_bytes);
         mbar_arrive_expect_tx(&full[s], bytes);
-        tma_load_3d(dst, &tmap, kc[a].ox, kc[a].oy, a, &full[s]);
+        tma_load_3d(dst, tmap, kc[a].ox, kc[a].oy, a, &full[s]);
         issued = a + 1;
       }
       // Drain: the last load issued into each stage must land before exit
@@ -164,7 +171,34 @@ bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
     const WinConst k = kc[a];
     const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
     const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
-    if (active) {
+    if (active && BZ0 && MODE == 1) {
+      // x is affine in z: the column's end voxels bound every tap index, so
+      // the window bound is checked once per column instead of per voxel.
+      const float fly = floorf(yr);
+      const float fy = yr - fly;
+      const int rowi = magic_int(fly) + k.lym;
+      const int ixa = magic_int(floorf(xr)) + k.lxm;
+      const int ixb = magic_int(floorf(fmaf(k.a3, (float)(NZ - 1), xr))) + k.lxm;
+      if ((unsigned)rowi >= lim_y || (unsigned)ixa >= lim_x || (unsigned)ixb >= lim_x) {
+        bad = true;
+      } else {
+        const PT* row0 = w + rowi * WX;
+        const float wy0 = 1.f - fy, wy1 = fy;
+#pragma unroll
+        for (int z = 0; z < NZ; ++z) {
+          const float x = fmaf(k.a3, (float)z, xr);
+          const float flx = floorf(x);
+          const float fx = x - flx;
+          const PT* p = row0 + (magic_int(flx) + k.lxm);
+          const float p00 = to_f(p[0]), p10 = to_f(p[1]);
+          const float p01 = to_f(p[WX]), p11 = to_f(p[WX + 1]);
+          const float r0 = fmaf(fx, p10 - p00, p00);
+          const float r1 = fmaf(fx, p11 - p01, p01);
+          s[z] = fmaf(wy0, r0, s[z]);
+          s[z] = fmaf(wy1, r1, s[z]);
+        }
+      }
+    } else if (active) {
       // y part (per column when the map has no Z term)
       float fy = 0.f, wy0 = 0.f, wy1 = 0.f, cy = 0.f;
       int rowi = 0;
@@ -247,9 +281,16 @@ bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   }
 }
 
-template <typename PT, int MODE, bool LANE_Y, bool BZ0>
+// One CTA per brick of one axis.
+template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
+__global__ void __launch_bounds__(kThreads)
+bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  bp_brick<PT, MODE, LANE_Y, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.y, blockIdx.z, smem, false);
+}
+
+template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
 cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cudaStream_t st) {
-  constexpr int NZ = 8;
   auto kern = bp_tma_kernel<PT, MODE, LANE_Y, BZ0, NZ>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -259,12 +300,74 @@ cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cud
   return cudaGetLastError();
 }
 
+template <typename PT, int MODE, bool LANE_Y, bool BZ0>
+cudaError_t launch_nz(const CUtensorMap& map, const BpArgs& P, const BpPlan& plan, cudaStream_t st) {
+  // WBP runs once per reconstruction: one brick depth.  SIRT: the tuned depth.
+  if (MODE == 0 || plan.nz == 8) return launch_one<PT, MODE, LANE_Y, BZ0, 8>(map, P, plan.smem, st);
+  if (plan.nz == 4) return launch_one<PT, MODE, LANE_Y, BZ0, 4>(map, P, plan.smem, st);
+  if (plan.nz == 16) return launch_one<PT, MODE, LANE_Y, BZ0, 16>(map, P, plan.smem, st);
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace
 
-// Window box for a brick of the given shape over all angles of an axis.
-BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half) {
+const int kBpDepths[3] = {4, 8, 16};
+
+namespace {
+
+// Persistent SIRT back-projection over the bricks of many axes: each CTA
+// takes items blockIdx.x, blockIdx.x + gridDim.x, ...; items are ordered by
+// cost (most angles first) so the tail is short.  Between items every warp
+// (producer included) meets at a barrier, then the mbarriers are
+// re-initialised for the next brick.
+__global__ void __launch_bounds__(kThreads)
+bp_batch_kernel(const BpBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items, int* err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int NZ = kBatchBpNZ;
+  bool first = true;
+  for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+    if (!first) __syncthreads();
+    const int2 item = items[it];
+    const BpBatchDesc& D = descs[item.x];
+    const BpArgs P{D.ax, D.vol, D.vol.Zs, D.vol.Zs + D.vol.NZ, D.WX, D.WY, D.align, 1, D.step, D.vol_out,
+                   const_cast<float*>(D.cbp), D.vol_copy, D.copy_kind, err};
+    const int bx = item.y % D.gx, by = (item.y / D.gx) % D.gy, bz = item.y / (D.gx * D.gy);
+    switch (D.lane_y * 2 + D.bz0) {
+      case 0: bp_brick<float, 1, false, false, NZ>(D.map, P, bx, by, bz, smem, !first); break;
+      case 1: bp_brick<float, 1, false, true, NZ>(D.map, P, bx, by, bz, smem, !first); break;
+      case 2: bp_brick<float, 1, true, false, NZ>(D.map, P, bx, by, bz, smem, !first); break;
+      default: bp_brick<float, 1, true, true, NZ>(D.map, P, bx, by, bz, smem, !first); break;
+    }
+    first = false;
+  }
+}
+
+}  // namespace
+
+int backproject_batch_ctas_per_sm(size_t smem) {
+  int n = 0;
+  if (cudaFuncSetAttribute(bp_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, bp_batch_kernel, kThreads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n > 0 ? n : 1;
+}
+
+cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const int2* items, long long n_items, size_t smem,
+                                     int grid, int* err, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(bp_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  bp_batch_kernel<<<grid, kThreads, smem, st>>>(descs, items, n_items, err);
+  return cudaGetLastError();
+}
+
+// Window box for a brick of depth nz over all angles of an axis.
+BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
+                        int lane) {
   BpPlan p;
   p.align = half ? 8 : 4;
+  p.nz = nz;
   // Choose the lane axis so that consecutive lanes step along detector x.
   double sx = 0, sy = 0;
   bool bz0 = true;
@@ -273,9 +376,9 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
     sy += std::fabs(xc[4 * a + 2]) - std::fabs(yc[4 * a + 2]);
     if (yc[4 * a + 3] != 0.0) bz0 = false;
   }
-  p.lane_y = sy > sx;
+  p.lane_y = lane < 0 ? sy > sx : lane == 1;  // lane: -1 heuristic, 0 along X, 1 along Y
   p.bz0 = bz0;
-  const int BX = p.lane_y ? kConsumerWarps : 32, BY = p.lane_y ? 32 : kConsumerWarps, BZ = 8;
+  const int BX = p.lane_y ? kConsumerWarps : 32, BY = p.lane_y ? 32 : kConsumerWarps, BZ = nz;
   double ex = 0, ey = 0;
   for (int a = 0; a < A; ++a) {
     ex = std::max(ex, std::fabs(xc[4 * a + 1]) * (BX - 1) + std::fabs(xc[4 * a + 2]) * (BY - 1) +
@@ -287,7 +390,7 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
   const int wx = (int)std::ceil(ex) + 4 + p.align;
   p.WX = (wx + p.align - 1) / p.align * p.align;
   p.WY = (int)std::ceil(ey) + 4;
-  p.ok = p.WX <= 256 && p.WY <= 256;
+  p.ok = p.WX <= 256 && p.WY <= 256 && (nz == 4 || nz == 8 || nz == 16);
   const size_t stage = (((size_t)p.WX * p.WY * (half ? 2 : 4)) + 127) & ~(size_t)127;
   p.smem = 128 + ((((size_t)A * sizeof(WinConst)) + 127) & ~(size_t)127) + NST * stage;
   if (p.smem > 227 * 1024) p.ok = false;
@@ -299,13 +402,19 @@ cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, c
                                    int mode, float step, float* vol_out, float* cbp, void* vol_copy, int copy_kind,
                                    int z0, int z1, int* err, cudaStream_t st) {
   BpArgs P{ax, vol, z0, z1, plan.WX, plan.WY, plan.align, mode, step, vol_out, cbp, vol_copy, copy_kind, err};
-#define MTR_BP_CASE(M, LY, BZ)                                                   \
-  if (mode == M && plan.lane_y == LY && plan.bz0 == BZ)                          \
-    return launch_one<PT, M, LY, BZ>(map, P, plan.smem, st);
-  MTR_BP_CASE(0, false, false) MTR_BP_CASE(0, false, true) MTR_BP_CASE(0, true, false) MTR_BP_CASE(0, true, true)
-  MTR_BP_CASE(1, false, false) MTR_BP_CASE(1, false, true) MTR_BP_CASE(1, true, false) MTR_BP_CASE(1, true, true)
-#undef MTR_BP_CASE
-  return cudaErrorInvalidValue;
+  if (mode == 0) {
+    if (!plan.lane_y && !plan.bz0) return launch_nz<PT, 0, false, false>(map, P, plan, st);
+    if (!plan.lane_y && plan.bz0) return launch_nz<PT, 0, false, true>(map, P, plan, st);
+    if (plan.lane_y && !plan.bz0) return launch_nz<PT, 0, true, false>(map, P, plan, st);
+    return launch_nz<PT, 0, true, true>(map, P, plan, st);
+  }
+  if constexpr (std::is_same<PT, float>::value) {
+    if (!plan.lane_y && !plan.bz0) return launch_nz<PT, 1, false, false>(map, P, plan, st);
+    if (!plan.lane_y && plan.bz0) return launch_nz<PT, 1, false, true>(map, P, plan, st);
+    if (plan.lane_y && !plan.bz0) return launch_nz<PT, 1, true, false>(map, P, plan, st);
+    return launch_nz<PT, 1, true, true>(map, P, plan, st);
+  }
+  return cudaErrorInvalidValue;  // the SIRT update reads the FP32 residual only
 }
 
 template cudaError_t launch_backproject_tma<float>(const CUtensorMap&, const BpPlan&, const AxisDev&, const VolDev&,

@@ -13,14 +13,20 @@
 //
 // Window accumulation is fixed point: shared-memory float atomicAdd is not a
 // single native operation on this part, integer adds are.  Each CTA scales
-// its voxels by a power of two S with S * max|v| < 2^b, b <= 21, so every tap
-// weight*value rounds to an integer below 2^21 (rounded with the 1.5*2^23
-// trick, no float->int conversion) with an absolute error of at most
-// 2^-(b+1) * max|v|.  The host bounds the weight one pixel can receive from
-// one brick by 2^mass_shift (lattice points in the preimage of a 2x2-pixel
-// square, times the brick depth) and b = min(21, 30 - mass_shift) keeps every
-// window sum below 2^30.  Before the flush the window is converted back to
-// float and divided by S (exact: S is a power of two).
+// its voxels by a power of two S with S * max|v| < 2^b, b <= 17, so every
+// added value (a tap, or a column's merged run of at most 16 voxels) rounds
+// to an integer below 2^21 (rounded with the 1.5*2^23 trick, no float->int
+// conversion) with an absolute error of at most 2^-(b+1) * max|v|.  The host
+// bounds the weight one pixel can receive from one brick by 2^mass_shift
+// (lattice points in the preimage of a 2x2-pixel square, times the brick
+// depth) and b <= 30 - mass_shift keeps every window sum below 2^30.  Before
+// the flush the window is converted back to float and divided by S (exact:
+// S is a power of two).
+//
+// When the y-map has no Z term, a voxel column's y weights are common to the
+// column and its x advances by |a3| < 1 per voxel: the interior path merges
+// the column's 1-D splat in registers and adds one value per pixel it leaves
+// (2-16x fewer shared-memory adds than four per voxel, depending on the tilt).
 //
 // Windows are clamped inside the detector (TMA reduces must not start at a
 // negative coordinate), so a tap is on the detector iff it lies in the valid
@@ -33,7 +39,6 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
-constexpr int kNZ = 16;
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
@@ -43,7 +48,8 @@ struct FwdConst {
   int lxm, lym;  // window-local integer base minus the magic bits
   int ox, oy;    // window origin (clamped inside the detector, ox aligned)
   int wlx;       // valid window columns (left of the detector's right edge)
-  int pad[3];
+  int interior;  // window not clamped and inside the detector: every tap is valid
+  int pad[2];
 };
 
 struct FwdArgs {
@@ -74,13 +80,52 @@ template <> __device__ __forceinline__ float ldv<__half>(const void* p, long lon
   return __half2float(__ldg(static_cast<const __half*>(p) + i));
 }
 
-template <typename VT, bool LANE_Y, bool BZ0>
-__global__ void __launch_bounds__(kThreads)
-fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
-  constexpr int NZ = kNZ;
+// Streaming splat of one voxel column (fixed X, Y; y-map without a Z term)
+// into detector rows `row` and `row + WX`.  x advances by |a3| < 1 per voxel,
+// so consecutive voxels reach at most one new pixel: the column's 1-D splat is
+// accumulated in registers and a pixel is emitted (one integer add per row,
+// its y weights wy0 / wy1 factored out of the column) only when the column
+// moves past it.  ASC walks z upwards (a3 >= 0), else downwards, so that x
+// never decreases.
+template <bool ASC, int NZ>
+__device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)[NZ], float xr, float a3, int lxm,
+                                              float wy0, float wy1) {
+  constexpr int zf = ASC ? 0 : NZ - 1;
+  float x = fmaf(a3, (float)zf, xr);
+  float flx = floorf(x);
+  float fx = x - flx;
+  int cur = magic_int(flx) + lxm;
+  float acc0 = (1.f - fx) * v[zf], acc1 = fx * v[zf];
+#pragma unroll
+  for (int i = 1; i < NZ; ++i) {
+    const int z = ASC ? i : NZ - 1 - i;
+    x = fmaf(a3, (float)z, xr);
+    flx = floorf(x);
+    fx = x - flx;
+    const int nxt = magic_int(flx) + lxm;
+    if (nxt != cur) {  // the column left pixel `cur` (nxt == cur + 1)
+      atomicAdd(row + cur, fixq(wy0, acc0));
+      atomicAdd(row + WX + cur, fixq(wy1, acc0));
+      acc0 = acc1;
+      acc1 = 0.f;
+      cur = nxt;
+    }
+    acc0 = fmaf(1.f - fx, v[z], acc0);
+    acc1 = fmaf(fx, v[z], acc1);
+  }
+  atomicAdd(row + cur, fixq(wy0, acc0));
+  atomicAdd(row + WX + cur, fixq(wy1, acc0));
+  atomicAdd(row + cur + 1, fixq(wy0, acc1));
+  atomicAdd(row + WX + cur + 1, fixq(wy1, acc1));
+}
+
+// One brick (bx, by, zb) and angle group g of one axis; `smem` is the CTA's
+// dynamic shared memory.  On return every bulk reduce it issued is complete.
+template <typename VT, bool LANE_Y, bool BZ0, int NZ>
+__device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs& P, int bx, int by, int zb, int g,
+                                          unsigned char* smem) {
   constexpr int BX = LANE_Y ? kWarps : 32;
   constexpr int BY = LANE_Y ? 32 : kWarps;
-  extern __shared__ __align__(128) unsigned char smem[];
   FwdConst* kc = reinterpret_cast<FwdConst*>(smem);
   const size_t kc_bytes = ((size_t)P.max_angles * sizeof(FwdConst) + 127) & ~(size_t)127;
   const int WX = P.WX, WY = P.WY;
@@ -90,12 +135,11 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
   float* red = reinterpret_cast<float*>(smem + kc_bytes);  // 32 floats for the block max
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int zb = blockIdx.z / P.groups, g = blockIdx.z % P.groups;
   const int A = P.ax.A;
   const int a_begin = (int)((long long)A * g / P.groups), a_end = (int)((long long)A * (g + 1) / P.groups);
   const int na = a_end - a_begin;
-  const int X0 = P.vol.Xs + blockIdx.x * BX;
-  const int Y0 = P.vol.Ys + blockIdx.y * BY;
+  const int X0 = P.vol.Xs + bx * BX;
+  const int Y0 = P.vol.Ys + by * BY;
   const int Z0 = P.z0 + zb * NZ;
   const int PX = P.ax.PX, PY = P.ax.PY;
 
@@ -114,16 +158,18 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
     const int xi = (int)fxb, yi = (int)fyb;
     const float xmin = k.xf + fminf(0.f, k.a1 * (BX - 1)) + fminf(0.f, k.a2 * (BY - 1)) + fminf(0.f, k.a3 * (NZ - 1));
     const float ymin = k.yf + fminf(0.f, k.b1 * (BX - 1)) + fminf(0.f, k.b2 * (BY - 1)) + fminf(0.f, k.b3 * (NZ - 1));
-    int ox = floor_div(xi + (int)floorf(xmin) - 1, 4) * 4;
-    int oy = yi + (int)floorf(ymin) - 1;
+    const int ox0 = floor_div(xi + (int)floorf(xmin) - 1, 4) * 4;
+    const int oy0 = yi + (int)floorf(ymin) - 1;
     // clamp inside [0, pitch - WX] x [0, PY - WY]; the host checked both ranges exist
-    ox = min(max(ox, 0), P.ax.pitch - WX);
-    oy = min(max(oy, 0), PY - WY);
+    const int ox = min(max(ox0, 0), P.ax.pitch - WX);
+    const int oy = min(max(oy0, 0), PY - WY);
     k.ox = ox;
     k.oy = oy;
     k.lxm = xi - ox - kMagicBits;
     k.lym = yi - oy - kMagicBits;
     k.wlx = min(WX, PX - ox);
+    // An unclamped window holds the whole footprint; inside the detector every tap is kept.
+    k.interior = (ox == ox0 && oy == oy0 && ox + WX <= PX) ? 1 : 0;
     kc[j] = k;
   }
 
@@ -149,16 +195,19 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
   __syncthreads();
   vmax = red[0];
   for (int w = 1; w < kWarps; ++w) vmax = fmaxf(vmax, red[w]);
-  // S = 2^(b-e) with vmax < 2^e: every |w*v*S| < 2^b <= 2^21 (magic rounding
-  // range) and a pixel's window sum < 2^(b + mass_shift) <= 2^30 (no overflow)
+  // S = 2^(b-e) with vmax < 2^e, so |v*S| < 2^b.  One emitted value merges at
+  // most NZ = 16 voxels of weight <= 1 each: |emission| < 2^(b+4) <= 2^21, the
+  // range of the magic rounding (b <= 17).  A pixel's window sum stays below
+  // 2^(b + mass_shift) <= 2^30 (no int overflow).
   int e2 = 0;
   if (vmax > 0.f && isfinite(vmax)) frexpf(vmax, &e2);
-  const int bits = min(21, 30 - P.mass_shift);
+  constexpr int kLog2NZ = NZ >= 32 ? 5 : NZ >= 16 ? 4 : 3;
+  const int bits = min(21 - kLog2NZ, 30 - P.mass_shift);
   const int sexp = max(-120, min(120, bits - e2));
   const float S = ldexpf(1.f, sexp), invS = ldexpf(1.f, -sexp);
 #pragma unroll
   for (int z = 0; z < NZ; ++z) v[z] *= S;
-  if (tid == 0) prefetch_tensormap(&smap);
+  if (tid == 0) prefetch_tensormap(smap);
 
   for (int j = 0; j < na; ++j) {
     const int a = a_begin + j;
@@ -175,7 +224,38 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
     }
     __syncthreads();
     const FwdConst k = kc[j];
-    if (active) {
+    if (active && BZ0 && k.interior && fabsf(k.a3) < 0.999f) {
+      // every tap lands in the window and on the detector; stream the column
+      const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
+      const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
+      const float fly = floorf(yr);
+      const float fy = yr - fly;
+      int* rowp = wi + (magic_int(fly) + k.lym) * WX;
+      if (k.a3 >= 0.f) stream_column<true, NZ>(rowp, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy);
+      else stream_column<false, NZ>(rowp, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy);
+    } else if (active && BZ0 && k.interior) {
+      // every tap lands in the window and on the detector: no per-tap tests
+      const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
+      const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
+      const float fly = floorf(yr);
+      const float fy = yr - fly;
+      const int rowi = magic_int(fly) + k.lym;
+      const float wy0 = 1.f - fy, wy1 = fy;
+      int* rowp = wi + rowi * WX;
+#pragma unroll
+      for (int z = 0; z < NZ; ++z) {
+        const float x = fmaf(k.a3, (float)z, xr);
+        const float flx = floorf(x);
+        const float fx = x - flx;
+        int* r0 = rowp + (magic_int(flx) + k.lxm);
+        const float g0 = wy0 * v[z], g1 = wy1 * v[z];
+        const float wx0 = 1.f - fx;
+        atomicAdd(r0, fixq(wx0, g0));
+        atomicAdd(r0 + 1, fixq(fx, g0));
+        atomicAdd(r0 + WX, fixq(wx0, g1));
+        atomicAdd(r0 + WX + 1, fixq(fx, g1));
+      }
+    } else if (active) {
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
       const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
       float wy0 = 0.f, wy1 = 0.f;
@@ -227,35 +307,117 @@ fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
     fence_proxy_async_smem();
     __syncthreads();
     if (tid == 0) {
-      tma_reduce_add_3d(&smap, wf, k.ox, k.oy, a);
+      tma_reduce_add_3d(smap, wf, k.ox, k.oy, a);
       bulk_commit();
     }
   }
   if (tid == 0) bulk_wait_all();
 }
 
-template <typename VT, bool LY, bool BZ>
+// One CTA per (brick, angle group) of one axis.
+template <typename VT, bool LANE_Y, bool BZ0, int NZ>
+__global__ void __launch_bounds__(kThreads)
+fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  fwd_brick<VT, LANE_Y, BZ0, NZ>(&smap, P, blockIdx.x, blockIdx.y, blockIdx.z / P.groups, blockIdx.z % P.groups,
+                                 smem);
+}
+
+template <typename VT, bool LY, bool BZ, int NZ>
 cudaError_t launch_one(const CUtensorMap& map, FwdArgs P, size_t smem, int num_sms, cudaStream_t st) {
-  auto kern = fwd_tma_kernel<VT, LY, BZ>;
+  auto kern = fwd_tma_kernel<VT, LY, BZ, NZ>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int BX = LY ? kWarps : 32, BY = LY ? 32 : kWarps;
   const long long bricks = (long long)((P.vol.NX + BX - 1) / BX) * ((P.vol.NY + BY - 1) / BY) *
-                           ((P.z1 - P.z0 + kNZ - 1) / kNZ);
+                           ((P.z1 - P.z0 + NZ - 1) / NZ);
   // split the angles over several CTAs when there are too few bricks to fill the GPU
   const long long target = (long long)num_sms * 8;
   int groups = (int)std::min<long long>((target + bricks - 1) / bricks, (long long)P.ax.A);
   if (groups < 1) groups = 1;
   P.groups = groups;
   P.max_angles = (P.ax.A + groups - 1) / groups;
-  const dim3 grid((P.vol.NX + BX - 1) / BX, (P.vol.NY + BY - 1) / BY, ((P.z1 - P.z0 + kNZ - 1) / kNZ) * groups);
+  const dim3 grid((P.vol.NX + BX - 1) / BX, (P.vol.NY + BY - 1) / BY, ((P.z1 - P.z0 + NZ - 1) / NZ) * groups);
   kern<<<grid, kThreads, smem, st>>>(map, P);
   return cudaGetLastError();
 }
 
+// Z-dependent y-maps take the per-tap path and use one depth.
+template <typename VT, bool LY, bool BZ>
+cudaError_t launch_nz(const CUtensorMap& map, const FwdArgs& P, const FwdPlan& plan, int sms, cudaStream_t st) {
+  if (!BZ || plan.nz == 16) return launch_one<VT, LY, BZ, 16>(map, P, plan.smem, sms, st);
+  if (plan.nz == 8) return launch_one<VT, LY, BZ, 8>(map, P, plan.smem, sms, st);
+  if (plan.nz == 32) return launch_one<VT, LY, BZ, 32>(map, P, plan.smem, sms, st);
+  return cudaErrorInvalidValue;
+}
+
 }  // namespace
 
-FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch) {
+const int kFwdDepths[3] = {8, 16, 32};
+
+namespace {
+
+// Persistent forward splat over the bricks of many axes (one angle group per
+// brick): each CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ...; every
+// brick ends with its bulk reduces complete, so the next one reuses the
+// shared-memory windows after a barrier.
+template <typename VT>
+__global__ void __launch_bounds__(kThreads)
+fwd_batch_kernel(const FwdBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  constexpr int NZ = kBatchFwdNZ;
+  bool first = true;
+  for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+    if (!first) __syncthreads();
+    const int2 item = items[it];
+    const FwdBatchDesc& D = descs[item.x];
+    const FwdArgs P{D.ax, D.vol, D.vol.Zs, D.vol.Zs + D.vol.NZ, D.WX, D.WY, 1, D.ax.A, D.mass_shift, D.x, nullptr};
+    const int bx = item.y % D.gx, by = (item.y / D.gx) % D.gy, bz = item.y / (D.gx * D.gy);
+    switch (D.lane_y * 2 + D.bz0) {
+      case 0: fwd_brick<VT, false, false, NZ>(D.map, P, bx, by, bz, 0, smem); break;
+      case 1: fwd_brick<VT, false, true, NZ>(D.map, P, bx, by, bz, 0, smem); break;
+      case 2: fwd_brick<VT, true, false, NZ>(D.map, P, bx, by, bz, 0, smem); break;
+      default: fwd_brick<VT, true, true, NZ>(D.map, P, bx, by, bz, 0, smem); break;
+    }
+    first = false;
+  }
+}
+
+}  // namespace
+
+template <typename VT>
+int forward_batch_ctas_per_sm(size_t smem) {
+  int n = 0;
+  if (cudaFuncSetAttribute(fwd_batch_kernel<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fwd_batch_kernel<VT>, kThreads, smem) != cudaSuccess) {
+    cudaGetLastError();
+    return 1;
+  }
+  return n > 0 ? n : 1;
+}
+
+template <typename VT>
+cudaError_t launch_forward_batch(const FwdBatchDesc* descs, const int2* items, long long n_items, size_t smem,
+                                 int grid, cudaStream_t st) {
+  cudaError_t e = cudaFuncSetAttribute(fwd_batch_kernel<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  fwd_batch_kernel<VT><<<grid, kThreads, smem, st>>>(descs, items, n_items);
+  return cudaGetLastError();
+}
+
+template int forward_batch_ctas_per_sm<float>(size_t);
+template int forward_batch_ctas_per_sm<__nv_bfloat16>(size_t);
+template int forward_batch_ctas_per_sm<__half>(size_t);
+template cudaError_t launch_forward_batch<float>(const FwdBatchDesc*, const int2*, long long, size_t, int,
+                                                 cudaStream_t);
+template cudaError_t launch_forward_batch<__nv_bfloat16>(const FwdBatchDesc*, const int2*, long long, size_t, int,
+                                                         cudaStream_t);
+template cudaError_t launch_forward_batch<__half>(const FwdBatchDesc*, const int2*, long long, size_t, int,
+                                                  cudaStream_t);
+
+FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch,
+                     int nz, int lane) {
   FwdPlan p;
   double sx = 0, sy = 0;
   bool bz0 = true;
@@ -264,9 +426,10 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
     sy += std::fabs(xc[4 * a + 2]) - std::fabs(yc[4 * a + 2]);
     if (yc[4 * a + 3] != 0.0) bz0 = false;
   }
-  p.lane_y = sy > sx;
+  p.lane_y = lane < 0 ? sy > sx : lane == 1;  // lane: -1 heuristic, 0 along X, 1 along Y
   p.bz0 = bz0;
-  const int BX = p.lane_y ? kWarps : 32, BY = p.lane_y ? 32 : kWarps, BZ = kNZ;
+  p.nz = bz0 ? nz : 16;  // Z-dependent y-maps use one depth
+  const int BX = p.lane_y ? kWarps : 32, BY = p.lane_y ? 32 : kWarps, BZ = p.nz;
   double ex = 0, ey = 0;
   for (int a = 0; a < A; ++a) {
     ex = std::max(ex, std::fabs(xc[4 * a + 1]) * (BX - 1) + std::fabs(xc[4 * a + 2]) * (BY - 1) +
@@ -294,7 +457,7 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
   }
   p.mass_shift = (int)std::ceil(std::log2(std::max(1.0, count * BZ)));
   p.ok = !singular && p.mass_shift <= 16 && p.WX <= 256 && p.WY <= 256 && p.WX <= pitch && p.WY <= PY &&
-         p.smem <= 200 * 1024;
+         p.smem <= 200 * 1024 && (p.nz == 8 || p.nz == 16 || p.nz == 32);
   (void)PX;
   return p;
 }
@@ -305,10 +468,10 @@ cudaError_t launch_forward_tma(const CUtensorMap& smap, const FwdPlan& plan, con
   int dev = 0, sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   FwdArgs P{ax, vol, z0, z1, plan.WX, plan.WY, 1, ax.A, plan.mass_shift, x, err};
-  if (!plan.lane_y && plan.bz0) return launch_one<VT, false, true>(smap, P, plan.smem, sms, st);
-  if (!plan.lane_y && !plan.bz0) return launch_one<VT, false, false>(smap, P, plan.smem, sms, st);
-  if (plan.lane_y && plan.bz0) return launch_one<VT, true, true>(smap, P, plan.smem, sms, st);
-  return launch_one<VT, true, false>(smap, P, plan.smem, sms, st);
+  if (!plan.lane_y && plan.bz0) return launch_nz<VT, false, true>(smap, P, plan, sms, st);
+  if (!plan.lane_y && !plan.bz0) return launch_nz<VT, false, false>(smap, P, plan, sms, st);
+  if (plan.lane_y && plan.bz0) return launch_nz<VT, true, true>(smap, P, plan, sms, st);
+  return launch_nz<VT, true, false>(smap, P, plan, sms, st);
 }
 
 template cudaError_t launch_forward_tma<float>(const CUtensorMap&, const FwdPlan&, const AxisDev&, const VolDev&,

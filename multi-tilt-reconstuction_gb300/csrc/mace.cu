@@ -116,7 +116,49 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
   }
 }
 
+// MACE step over many reconstructions: item = (descriptor, chunk of voxels);
+// the arithmetic is mace_kernel's (reference float rounding, FP64 consensus).
+__global__ void __launch_bounds__(kThreads)
+mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items) {
+  for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int2 item = items[it];
+    const MaceBatchDesc& D = descs[item.x];
+    const long long i0 = (long long)item.y * kBatchChunk;
+    const long long i1 = min(D.n, i0 + kBatchChunk);
+    const int K = D.K;
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      const float wa = D.wavg[i];
+      float wn[kMaxK];
+      double sum = 0.0;
+#pragma unroll
+      for (int k = 0; k < kMaxK; ++k) {
+        if (k < K) {
+          const float wk = D.w[k][i];
+          wn[k] = mann(D.x[k][i], __fsub_rn(2.f * wa, wk), wk, D.rho);
+          D.w[k][i] = wn[k];
+          sum += (double)wn[k];
+        }
+      }
+      const float na = (float)(sum / (double)K);
+      D.wavg[i] = na;
+#pragma unroll
+      for (int k = 0; k < kMaxK; ++k) {
+        if (k < K) {
+          const float zn = __fsub_rn(2.f * na, wn[k]);
+          D.x[k][i] = zn;
+          if (D.copy_kind == 1) static_cast<__nv_bfloat16*>(D.xc[k])[i] = __float2bfloat16_rn(zn);
+          else if (D.copy_kind == 2) static_cast<__half*>(D.xc[k])[i] = __float2half_rn(zn);
+        }
+      }
+    }
+  }
+}
+
 }  // namespace
+
+void launch_mace_batch(const MaceBatchDesc* descs, const int2* items, long long n_items, int grid, cudaStream_t st) {
+  mace_batch_kernel<<<grid, kThreads, 0, st>>>(descs, items, n_items);
+}
 
 void launch_fill(float* p, long long n, float v, cudaStream_t st) {
   fill_kernel<<<grid_for(n), kThreads, 0, st>>>(p, n, v);

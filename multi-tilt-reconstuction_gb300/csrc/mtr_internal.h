@@ -72,9 +72,13 @@ struct BpPlan {
   bool bz0 = false;    // y map independent of Z for every angle
   int WX = 0, WY = 0;  // window box (elements)
   int align = 4;       // TMA x alignment (elements)
+  int nz = 8;          // brick depth (voxels per thread along Z): 4, 8 or 16
   size_t smem = 0;     // dynamic shared memory per CTA
 };
-BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half);
+extern const int kBpDepths[3];  // candidate brick depths of the SIRT back-projection
+// lane: -1 picks the lane axis along the larger x-map slope, 0 = X, 1 = Y.
+BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
+                        int lane = -1);
 template <typename PT>
 cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, const AxisDev& ax,
                                    const VolDev& vol, int mode, float step, float* vol_out, float* cbp,
@@ -92,12 +96,74 @@ struct FwdPlan {
   bool bz0 = false;
   int WX = 0, WY = 0;
   int mass_shift = 0;  // log2 bound of a pixel's weight from one brick
+  int nz = 16;         // brick depth: 8, 16 or 32
   size_t smem = 0;
 };
-FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch);
+extern const int kFwdDepths[3];  // candidate brick depths of the forward splat
+FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch,
+                     int nz, int lane = -1);
 template <typename VT>
 cudaError_t launch_forward_tma(const CUtensorMap& smap, const FwdPlan& plan, const AxisDev& ax, const VolDev& vol,
                                const VT* x, int z0, int z1, int* err, cudaStream_t st);
+
+// ---- persistent batched launches over many axes (batch.cu) -----------------
+// One descriptor per (instance, axis); one work item per brick, (descriptor,
+// brick index).  The kernels' CTAs loop over items (a grid sized to the GPU).
+struct BpBatchDesc {
+  AxisDev ax;
+  VolDev vol;
+  int WX, WY, align;
+  int gx, gy;            // brick grid in X and Y
+  int lane_y, bz0;
+  float step;
+  float* vol_out;        // SIRT iterate (updated in place)
+  const float* cbp;      // back-projection weight sums
+  void* vol_copy;        // bf16/f16 copy (mixed) or null
+  int copy_kind;
+  const CUtensorMap* map;  // device address of the residual's tensor map
+};
+struct FwdBatchDesc {
+  AxisDev ax;
+  VolDev vol;
+  int WX, WY, mass_shift;
+  int gx, gy;
+  int lane_y, bz0;
+  const void* x;         // volume read by the splat (float / bf16 / f16)
+  const CUtensorMap* map;  // device address of the ray-sum tensor map
+};
+struct ResBatchDesc {
+  const void* b;         // projections (float or half)
+  float* s;
+  const float* cf;
+  float* r;
+  long long n;
+};
+struct MaceBatchDesc {
+  int K;
+  float* w[MTR_MAX_AXES];
+  float* x[MTR_MAX_AXES];
+  void* xc[MTR_MAX_AXES];
+  float* wavg;
+  long long n;
+  float rho;
+  int copy_kind;
+};
+constexpr int kBatchChunk = 1 << 16;  // elements per residual / MACE work item
+
+// NZ: brick depth of the batch (8 for the back-projection, 16 for the forward).
+cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const int2* items, long long n_items, size_t smem,
+                                     int grid, int* err, cudaStream_t st);
+template <typename VT>
+cudaError_t launch_forward_batch(const FwdBatchDesc* descs, const int2* items, long long n_items, size_t smem,
+                                 int grid, cudaStream_t st);
+int backproject_batch_ctas_per_sm(size_t smem);
+template <typename VT>
+int forward_batch_ctas_per_sm(size_t smem);
+constexpr int kBatchBpNZ = 8;
+constexpr int kBatchFwdNZ = 16;
+void launch_residual_batch(const ResBatchDesc* descs, const int2* items, long long n_items, int half_b, int grid,
+                           cudaStream_t st);
+void launch_mace_batch(const MaceBatchDesc* descs, const int2* items, long long n_items, int grid, cudaStream_t st);
 
 // ---- elementwise / MACE (mace.cu) ----------------------------------------
 void launch_fill(float* p, long long n, float v, cudaStream_t st);

@@ -126,9 +126,10 @@ struct AxisState {
   int pitch = 0;          // row pitch of projection-space arrays (elements)
   long long np = 0;       // A*PY*pitch
   std::vector<double> hxc, hyc;  // host copies of the maps (kernel planning)
-  BpPlan plan;            // TMA back-projection window plan
-  CUtensorMap map_b{}, map_r{};  // tensor maps over b and r (valid when tma)
-  bool tma = false;
+  BpPlan plan;            // TMA back-projection window plan over r (FP32)
+  BpPlan plan_b;          // ... over b (fp16 when mixed), for the WBP
+  CUtensorMap map_b{}, map_r{};  // tensor maps over b and r
+  bool tma = false, tma_b = false;
   FwdPlan fplan;          // windowed forward splat plan
   CUtensorMap map_s{}, map_cf{};  // tensor maps over s and cf (valid when ftma)
   bool ftma = false;
@@ -147,6 +148,24 @@ struct AxisState {
 // Disable the TMA kernels (MTR_DISABLE_TMA=1 in the environment) to run the
 // plain global-memory kernels instead; used to cross-check the two paths.
 bool tma_disabled();
+
+// Autotuner (tune.cu): picks the brick depths of the SIRT back-projection and
+// the forward splat for one axis, timing candidates on the axis' buffers
+// before they hold data, and encodes the tensor maps.
+bool autotune_enabled();
+bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, float* scratch_vol,
+               float* scratch_cbp, int* err);
+
+}  // namespace mtr
+
+struct mtr_recon;
+namespace mtr {
+// WBP sum into w_avg, w_k = z_k = w_avg, records reset (recon.cu).
+mtr_status recon_enqueue_init(mtr_recon* r);
+// One SIRT phase of axis k of a reconstruction, with its own kernels.
+mtr_status recon_enqueue_forward(mtr_recon* r, int k);
+mtr_status recon_enqueue_residual(mtr_recon* r, int k);
+mtr_status recon_enqueue_sirt_bp(mtr_recon* r, int k);
 
 }  // namespace mtr
 

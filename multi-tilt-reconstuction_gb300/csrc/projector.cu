@@ -232,6 +232,26 @@ residual_kernel(long long n, const BT* __restrict__ b, float* __restrict__ s, co
   }
 }
 
+// Residual over many axes: item = (descriptor, chunk of kBatchChunk pixels).
+template <bool HALF_B>
+__global__ void __launch_bounds__(256)
+residual_batch_kernel(const ResBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items) {
+  for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int2 item = items[it];
+    const ResBatchDesc& D = descs[item.x];
+    const long long i0 = (long long)item.y * kBatchChunk;
+    const long long i1 = min(D.n, i0 + kBatchChunk);
+    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
+      float sv = D.s[i];
+      const float cv = D.cf[i];
+      if (cv != 0.f) sv = sv / cv;
+      const float bv = HALF_B ? __half2float(static_cast<const __half*>(D.b)[i]) : static_cast<const float*>(D.b)[i];
+      D.r[i] = bv - sv;
+      D.s[i] = 0.f;
+    }
+  }
+}
+
 dim3 vol_grid(const VolDev& vol, int z0, int z1) {
   return dim3((vol.NX + kTX - 1) / kTX, (vol.NY + kTY - 1) / kTY, (z1 - z0 + kZR - 1) / kZR);
 }
@@ -267,6 +287,12 @@ void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, 
   residual_kernel<BT, RT><<<(unsigned)blocks, 256, 0, st>>>(n, b, s, c, r, norm2);
 }
 
+void launch_residual_batch(const ResBatchDesc* descs, const int2* items, long long n_items, int half_b, int grid,
+                           cudaStream_t st) {
+  if (half_b) residual_batch_kernel<true><<<grid, 256, 0, st>>>(descs, items, n_items);
+  else residual_batch_kernel<false><<<grid, 256, 0, st>>>(descs, items, n_items);
+}
+
 template void launch_backproject<float>(const AxisDev&, const VolDev&, const float*, int, float, float*, float*,
                                         void*, int, int, int, cudaStream_t);
 template void launch_backproject<__half>(const AxisDev&, const VolDev&, const __half*, int, float, float*, float*,
@@ -277,7 +303,7 @@ template void launch_forward<__nv_bfloat16>(const AxisDev&, const VolDev&, const
 template void launch_forward<__half>(const AxisDev&, const VolDev&, const __half*, float*, int, int, cudaStream_t);
 template void launch_residual<float, float>(long long, const float*, float*, const float*, float*, double*,
                                             cudaStream_t);
-template void launch_residual<__half, __half>(long long, const __half*, float*, const float*, __half*, double*,
-                                              cudaStream_t);
+template void launch_residual<__half, float>(long long, const __half*, float*, const float*, float*, double*,
+                                             cudaStream_t);
 
 }  // namespace mtr

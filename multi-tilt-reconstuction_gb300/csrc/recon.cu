@@ -39,7 +39,7 @@ long long axis_bytes(long long np, long long nv, int precision) {
   b += np * pe;       // b
   b += np * 4;        // s
   b += np * 4;        // cf
-  b += np * pe;       // r
+  b += np * 4;        // r (FP32 in every mode: the back-projection reads it per tap)
   b += nv * 4 * 3;    // cbp, w, x
   if (mixed(precision)) b += nv * 2;  // xcopy
   return b;
@@ -124,8 +124,8 @@ mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
   mtr_context* ctx = r->ctx;
   ProfScope ps(ctx, MTR_KERNEL_RESIDUAL);
   if (mixed(r->p.precision))
-    launch_residual<__half, __half>(a.np, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<__half>(), norm,
-                                    ctx->stream);
+    launch_residual<__half, float>(a.np, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), norm,
+                                   ctx->stream);
   else
     launch_residual<float, float>(a.np, a.b.as<float>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), norm,
                                   ctx->stream);
@@ -139,23 +139,27 @@ mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const void* img_f32_
   const int z0 = v.Zs, z1 = v.Zs + v.NZ;
   const int ck = copy_kind_of(r->p.precision);
   ProfScope ps(ctx, mode == 0 ? MTR_KERNEL_WBP : MTR_KERNEL_BACKPROJECT);
-  if (a.tma && !img_f32_or_null) {
-    const CUtensorMap& map = mode == 0 ? a.map_b : a.map_r;
+  // WBP reads the projections (fp16 when mixed), SIRT reads the FP32 residual.
+  const bool half_img = mode == 0 && mixed(r->p.precision);
+  if ((mode == 0 ? a.tma_b : a.tma) && !img_f32_or_null) {
     cudaError_t e;
-    if (mixed(r->p.precision))
-      e = launch_backproject_tma<__half>(map, a.plan, a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
+    if (half_img)
+      e = launch_backproject_tma<__half>(a.map_b, a.plan_b, a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
                                          a.cbp.as<float>(), a.xcopy.p, ck, z0, z1, r->err.as<int>(), ctx->stream);
     else
-      e = launch_backproject_tma<float>(map, a.plan, a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
-                                        a.cbp.as<float>(), nullptr, 0, z0, z1, r->err.as<int>(), ctx->stream);
+      e = launch_backproject_tma<float>(mode == 0 ? a.map_b : a.map_r, mode == 0 ? a.plan_b : a.plan, a.dev(), v,
+                                        mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(), a.xcopy.p, ck, z0,
+                                        z1, r->err.as<int>(), ctx->stream);
     g_launches.fetch_add(1);
     if (e != cudaSuccess) return cuda_error(ctx, e, "tma back-projection");
     return MTR_OK;
   }
-  if (mixed(r->p.precision)) {
-    const __half* img = mode == 0 ? a.b.as<__half>() : a.r.as<__half>();
-    launch_backproject<__half>(a.dev(), v, img, mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(),
-                               a.xcopy.p, ck, z0, z1, ctx->stream);
+  if (half_img) {
+    launch_backproject<__half>(a.dev(), v, a.b.as<__half>(), mode, r->p.sirt_step, a.x.as<float>(),
+                               a.cbp.as<float>(), a.xcopy.p, ck, z0, z1, ctx->stream);
+  } else if (mixed(r->p.precision)) {
+    launch_backproject<float>(a.dev(), v, a.r.as<float>(), mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(),
+                              a.xcopy.p, ck, z0, z1, ctx->stream);
   } else {
     const float* img = mode == 0 ? a.b.as<float>() : a.r.as<float>();
     if (img_f32_or_null) img = static_cast<const float*>(img_f32_or_null);
@@ -166,8 +170,11 @@ mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const void* img_f32_
   return MTR_OK;
 }
 
-// WBP init, w_k = z_k = x0 sum, then the MACE loop.
-mtr_status enqueue_run(mtr_recon* r) {
+}  // namespace
+
+// WBP init: w_avg = sum of per-axis WBPs, w_k = z_k = w_avg (and the
+// forward-read copies), norms and change records reset.
+mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
   mtr_context* ctx = r->ctx;
   const long long nv = r->nv;
   const size_t vbytes = (size_t)nv * 4;
@@ -198,6 +205,26 @@ mtr_status enqueue_run(mtr_recon* r) {
   double* dch = r->dchange.as<double>();
   if (norms) MTR_CK(ctx, cudaMemsetAsync(norms, 0, sizeof(double) * (size_t)no * K * ni, ctx->stream));
   if (dch) MTR_CK(ctx, cudaMemsetAsync(dch, 0, sizeof(double) * (size_t)no, ctx->stream));
+  return MTR_OK;
+}
+
+mtr_status mtr::recon_enqueue_forward(mtr_recon* r, int k) { return enqueue_forward(r, r->ax[k]); }
+mtr_status mtr::recon_enqueue_residual(mtr_recon* r, int k) { return enqueue_residual(r, r->ax[k], nullptr); }
+mtr_status mtr::recon_enqueue_sirt_bp(mtr_recon* r, int k) { return enqueue_bp(r, r->ax[k], 1, nullptr); }
+
+namespace {
+
+// WBP init, then the MACE loop.
+mtr_status enqueue_run(mtr_recon* r) {
+  mtr_status st = recon_enqueue_init(r);
+  if (st != MTR_OK) return st;
+  mtr_context* ctx = r->ctx;
+  const long long nv = r->nv;
+  const int ck = copy_kind_of(r->p.precision);
+  float* wavg = r->wavg.as<float>();
+  const int K = r->K, ni = r->p.sirt_inner, no = r->p.iter_times;
+  double* norms = r->norms.as<double>();
+  double* dch = r->dchange.as<double>();
   std::vector<float*> ws(K), xs(K);
   std::vector<void*> xcs(K);
   for (int k = 0; k < K; ++k) {
@@ -290,7 +317,7 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     MTR_CK(ctx, a.b.alloc((size_t)a.np * pe));
     MTR_CK(ctx, a.s.alloc((size_t)a.np * 4));
     MTR_CK(ctx, a.cf.alloc((size_t)a.np * 4));
-    MTR_CK(ctx, a.r.alloc((size_t)a.np * pe));
+    MTR_CK(ctx, a.r.alloc((size_t)a.np * 4));
     MTR_CK(ctx, a.cbp.alloc(vb));
     MTR_CK(ctx, a.w.alloc(vb));
     MTR_CK(ctx, a.x.alloc(vb));
@@ -299,19 +326,16 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     MTR_CK(ctx, cudaMemcpyAsync(a.xc.p, axes[k].x_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemcpyAsync(a.yc.p, axes[k].y_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream));
-    MTR_CK(ctx, cudaMemsetAsync(a.r.p, 0, (size_t)a.np * pe, ctx->stream));
+    MTR_CK(ctx, cudaMemsetAsync(a.r.p, 0, (size_t)a.np * 4, ctx->stream));
     s = upload_projections(r.get(), k, axes[k].prj_data, mem_kind);
     if (s != MTR_OK) return s;
     // TMA kernels where the window geometry fits (else the plain kernels run).
     if (!tma_disabled()) {
-      a.plan = plan_backproject(a.hxc, a.hyc, a.A, mx);
-      a.tma = a.plan.ok &&
-              encode_tensor_map_3d(&a.map_b, a.b.p, mx, a.PX, a.pitch, a.PY, a.A, a.plan.WX, a.plan.WY) &&
-              encode_tensor_map_3d(&a.map_r, a.r.p, mx, a.PX, a.pitch, a.PY, a.A, a.plan.WX, a.plan.WY);
-      a.fplan = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch);
-      a.ftma = a.fplan.ok &&
-               encode_tensor_map_3d(&a.map_s, a.s.p, false, a.pitch, a.pitch, a.PY, a.A, a.fplan.WX, a.fplan.WY) &&
-               encode_tensor_map_3d(&a.map_cf, a.cf.p, false, a.pitch, a.pitch, a.PY, a.A, a.fplan.WX, a.fplan.WY);
+      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, mx, 8);  // WBP over b (fp16 when mixed)
+      a.tma_b = a.plan_b.ok &&
+                encode_tensor_map_3d(&a.map_b, a.b.p, mx, a.PX, a.pitch, a.PY, a.A, a.plan_b.WX, a.plan_b.WY);
+      // SIRT back-projection over the FP32 residual and the forward splat: tuned depths
+      tune_axis(ctx, a, r->vol, params->precision, a.w.as<float>(), a.cbp.as<float>(), r->err.as<int>());
     }
   }
   if (params->flags & MTR_FLAG_RECORD_NORMS) {
@@ -416,6 +440,25 @@ mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n) {
 mtr_status mtr_recon_footprint(const mtr_recon* r, long long* bytes) {
   if (!r || !bytes) return MTR_ERR_INVALID_ARGUMENT;
   *bytes = r->bytes;
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_describe(const mtr_recon* r, char* buf, int cap) {
+  if (!r || !buf || cap <= 0) return MTR_ERR_INVALID_ARGUMENT;
+  std::string s = "[";
+  for (size_t k = 0; k < r->ax.size(); ++k) {
+    const AxisState& a = r->ax[k];
+    char t[512];
+    std::snprintf(t, sizeof(t),
+                  "%s{\"axis\":%zu,\"back_projection\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\"},"
+                  "\"forward\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\",\"y_has_z\":%s}}",
+                  k ? "," : "", k, a.tma ? "true" : "false", a.plan.nz, a.plan.WX, a.plan.WY,
+                  a.plan.lane_y ? "y" : "x", a.ftma ? "true" : "false", a.fplan.nz, a.fplan.WX, a.fplan.WY,
+                  a.fplan.lane_y ? "y" : "x", a.fplan.bz0 ? "false" : "true");
+    s += t;
+  }
+  s += "]";
+  std::snprintf(buf, (size_t)cap, "%s", s.c_str());
   return MTR_OK;
 }
 

@@ -1,0 +1,210 @@
+// Autotuner for the projector tile shapes.
+//
+// Two shape parameters decide the projectors' speed and depend on the
+// geometry:
+//  * brick depth (voxels per thread along Z): deep bricks amortise the
+//    per-angle window work and, in the forward splat, merge more of a
+//    column's taps; shallow bricks give more CTAs on small volumes and use
+//    fewer registers;
+//  * lane axis: lanes along X keep volume accesses coalesced, lanes along the
+//    volume axis that detector x follows keep shared-memory gathers free of
+//    bank conflicts.
+// For each tilt axis the tuner times every candidate (depth 4/8/16 x lane X/Y
+// for the SIRT back-projection, depth 8/16/32 x lane X/Y for the forward
+// splat) with CUDA events on the reconstruction's own buffers, before they
+// hold data (each candidate launch writes only scratch that the run
+// overwrites), and keeps the fastest.  Results are cached per process by a
+// geometry key and, when MTR_AUTOTUNE_CACHE names a file, persisted there as
+// JSON ({"key": [bp_depth, fwd_depth, bp_lane, fwd_lane], ...}).
+// MTR_AUTOTUNE=0 disables tuning (depths 8 and 16, lane axis by slope);
+// MTR_FORCE_DEPTHS=bp,fwd[,bp_lane,fwd_lane] pins the choice.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+
+#include "mtr_internal.h"
+#include "mtr_runtime.h"
+
+namespace mtr {
+namespace {
+
+struct Choice {
+  int bp_nz = 8, fwd_nz = 16, bp_lane = -1, fwd_lane = -1;
+};
+
+std::mutex g_mu;
+std::map<std::string, Choice> g_cache;
+bool g_loaded = false;
+
+const char* cache_path() {
+  const char* p = std::getenv("MTR_AUTOTUNE_CACHE");
+  return (p && *p) ? p : nullptr;
+}
+
+void load_file() {
+  if (g_loaded) return;
+  g_loaded = true;
+  const char* path = cache_path();
+  if (!path) return;
+  std::ifstream f(path);
+  if (!f) return;
+  std::stringstream ss;
+  ss << f.rdbuf();
+  const std::string s = ss.str();
+  // minimal parser for {"key": [a, b, c, d], ...} as written by save_file()
+  size_t i = 0;
+  while ((i = s.find('"', i)) != std::string::npos) {
+    const size_t j = s.find('"', i + 1);
+    if (j == std::string::npos) break;
+    const std::string key = s.substr(i + 1, j - i - 1);
+    const size_t lb = s.find('[', j), rb = s.find(']', j);
+    if (lb == std::string::npos || rb == std::string::npos) break;
+    Choice c;
+    if (std::sscanf(s.c_str() + lb, "[%d , %d , %d , %d]", &c.bp_nz, &c.fwd_nz, &c.bp_lane, &c.fwd_lane) == 4)
+      g_cache[key] = c;
+    i = rb + 1;
+  }
+}
+
+void save_file() {
+  const char* path = cache_path();
+  if (!path) return;
+  std::ofstream f(path, std::ios::trunc);
+  if (!f) return;
+  f << "{\n";
+  size_t n = 0;
+  for (const auto& kv : g_cache)
+    f << "  \"" << kv.first << "\": [" << kv.second.bp_nz << ", " << kv.second.fwd_nz << ", " << kv.second.bp_lane
+      << ", " << kv.second.fwd_lane << "]" << (++n < g_cache.size() ? ",\n" : "\n");
+  f << "}\n";
+}
+
+std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
+  double m[6] = {0, 0, 0, 0, 0, 0};
+  bool bz0 = true;
+  for (int k = 0; k < a.A; ++k) {
+    for (int c = 0; c < 3; ++c) m[c] = std::max(m[c], std::fabs(a.hxc[4 * k + 1 + c]));
+    for (int c = 0; c < 3; ++c) m[3 + c] = std::max(m[3 + c], std::fabs(a.hyc[4 * k + 1 + c]));
+    if (a.hyc[4 * k + 3] != 0.0) bz0 = false;
+  }
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d", a.PX, a.PY, a.A,
+                v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
+  return buf;
+}
+
+float time_launches(cudaStream_t st, const std::function<cudaError_t()>& launch, bool* ok) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  *ok = false;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return 0.f;
+  float ms = 0.f;
+  if (launch() == cudaSuccess) {  // warm-up (module load, attribute set-up)
+    cudaEventRecord(e0, st);
+    const cudaError_t e = launch();
+    cudaEventRecord(e1, st);
+    if (e == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
+      *ok = true;
+  }
+  cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return ms;
+}
+
+}  // namespace
+
+bool autotune_enabled() {
+  const char* e = std::getenv("MTR_AUTOTUNE");
+  return !(e && e[0] == '0');
+}
+
+// Chooses a.plan (SIRT back-projection over r) and a.fplan (forward splat
+// over s) for one axis and encodes the matching tensor maps.  Leaves s zeroed.
+bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, float* scratch_vol,
+               float* scratch_cbp, int* err) {
+  const int copy_kind = precision == MTR_PREC_MIXED_BF16 ? 1 : precision == MTR_PREC_MIXED_FP16 ? 2 : 0;
+  const std::string key = geometry_key(a, v, precision);
+  Choice ch;
+  bool known = false;
+  if (const char* f = std::getenv("MTR_FORCE_DEPTHS")) {
+    Choice c;
+    const int n = std::sscanf(f, "%d,%d,%d,%d", &c.bp_nz, &c.fwd_nz, &c.bp_lane, &c.fwd_lane);
+    if (n >= 2) {
+      if (n < 4) c.bp_lane = c.fwd_lane = -1;
+      ch = c;
+      known = true;
+    }
+  }
+  if (!known) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    load_file();
+    auto it = g_cache.find(key);
+    if (it != g_cache.end()) {
+      ch = it->second;
+      known = true;
+    }
+  }
+  const int z0 = v.Zs, z1 = v.Zs + v.NZ;
+  if (!known && autotune_enabled()) {
+    float best = 1e30f;
+    for (int lane = 0; lane < 2; ++lane)
+      for (int nz : kBpDepths) {
+        BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, false, nz, lane);
+        CUtensorMap m;
+        if (!p.ok || !encode_tensor_map_3d(&m, a.r.p, false, a.PX, a.pitch, a.PY, a.A, p.WX, p.WY)) continue;
+        bool ok = false;
+        const float ms = time_launches(ctx->stream, [&] {
+          return launch_backproject_tma<float>(m, p, a.dev(), v, 1, 0.5f, scratch_vol, scratch_cbp, a.xcopy.p,
+                                               copy_kind, z0, z1, err, ctx->stream);
+        }, &ok);
+        if (ok && ms < best) {
+          best = ms;
+          ch.bp_nz = nz;
+          ch.bp_lane = lane;
+        }
+      }
+    best = 1e30f;
+    for (int lane = 0; lane < 2; ++lane)
+      for (int nz : kFwdDepths) {
+        FwdPlan p = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, nz, lane);
+        CUtensorMap m;
+        if (!p.ok || p.nz != nz || !encode_tensor_map_3d(&m, a.s.p, false, a.pitch, a.pitch, a.PY, a.A, p.WX, p.WY))
+          continue;
+        bool ok = false;
+        const float ms = time_launches(ctx->stream, [&] {
+          if (copy_kind == 1)
+            return launch_forward_tma<__nv_bfloat16>(m, p, a.dev(), v, a.xcopy.as<__nv_bfloat16>(), z0, z1, err,
+                                                     ctx->stream);
+          if (copy_kind == 2)
+            return launch_forward_tma<__half>(m, p, a.dev(), v, a.xcopy.as<__half>(), z0, z1, err, ctx->stream);
+          return launch_forward_tma<float>(m, p, a.dev(), v, a.x.as<float>(), z0, z1, err, ctx->stream);
+        }, &ok);
+        if (ok && ms < best) {
+          best = ms;
+          ch.fwd_nz = nz;
+          ch.fwd_lane = lane;
+        }
+      }
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_cache[key] = ch;
+    save_file();
+  }
+  // the timing runs wrote into s and the tuner's scratch: restore the zeros
+  cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream);
+  a.plan = plan_backproject(a.hxc, a.hyc, a.A, false, ch.bp_nz, ch.bp_lane);
+  a.tma = a.plan.ok &&
+          encode_tensor_map_3d(&a.map_r, a.r.p, false, a.PX, a.pitch, a.PY, a.A, a.plan.WX, a.plan.WY);
+  a.fplan = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, ch.fwd_nz, ch.fwd_lane);
+  a.ftma = a.fplan.ok &&
+           encode_tensor_map_3d(&a.map_s, a.s.p, false, a.pitch, a.pitch, a.PY, a.A, a.fplan.WX, a.fplan.WY) &&
+           encode_tensor_map_3d(&a.map_cf, a.cf.p, false, a.pitch, a.pitch, a.PY, a.A, a.fplan.WX, a.fplan.WY);
+  return a.tma || a.ftma;
+}
+
+}  // namespace mtr

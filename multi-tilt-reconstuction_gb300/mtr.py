@@ -61,6 +61,10 @@ class AxisC(C.Structure):
                 ("prj_data", C.c_void_p)]
 
 
+class InstanceC(C.Structure):
+    _fields_ = [("n_axes", C.c_int), ("axes", C.POINTER(AxisC)), ("vol", VolumeSize)]
+
+
 class Params(C.Structure):
     _fields_ = [("iter_times", C.c_int), ("sirt_inner", C.c_int), ("sirt_step", C.c_float),
                 ("mace_step", C.c_float), ("precision", C.c_int), ("flags", C.c_int)]
@@ -121,9 +125,15 @@ _SIGNATURES = {
     "mtr_recon_check": (C.c_int, [_P]),
     "mtr_recon_norms": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong]),
     "mtr_recon_footprint": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "mtr_recon_describe": (C.c_int, [_P, C.c_char_p, C.c_int]),
     "mtr_recon_destroy": (C.c_int, [_P]),
     "mtr_estimate_footprint": (C.c_int, [C.c_int, C.POINTER(ProjectionSize), VolumeSize, C.c_int,
                                          C.POINTER(C.c_longlong)]),
+    "mtr_batch_create": (C.c_int, [_P, C.c_int, C.POINTER(InstanceC), C.POINTER(Params), C.c_int, C.POINTER(_P)]),
+    "mtr_batch_run": (C.c_int, [_P]),
+    "mtr_batch_download": (C.c_int, [_P, C.c_int, _P, C.c_int]),
+    "mtr_batch_info": (C.c_int, [_P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
+    "mtr_batch_destroy": (C.c_int, [_P]),
     "mtr_mrc_read_header": (C.c_int, [C.c_char_p, C.POINTER(MrcHeader)]),
     "mtr_mrc_read_stack": (C.c_int, [C.c_char_p, _P, C.c_longlong]),
     "mtr_txbr_read": (C.c_int, [C.c_char_p, _P, _P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -329,6 +339,14 @@ class Recon:
         self.ctx.check(self.ctx.lib.mtr_recon_norms(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), n), "norms")
         return out.reshape(self.p.iter_times, self.K, self.p.sirt_inner)
 
+    def describe(self) -> list:
+        """Kernels and tile shapes chosen per axis (JSON from mtr_recon_describe)."""
+        import json
+
+        buf = C.create_string_buffer(8192)
+        self.ctx.check(self.ctx.lib.mtr_recon_describe(self.h, buf, len(buf)), "describe")
+        return json.loads(buf.value.decode())
+
     def footprint(self) -> int:
         b = C.c_longlong()
         self.ctx.check(self.ctx.lib.mtr_recon_footprint(self.h, C.byref(b)), "footprint")
@@ -337,6 +355,52 @@ class Recon:
     def close(self) -> None:
         if self.h:
             self.ctx.lib.mtr_recon_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Many reconstructions run together (mtr_batch_*): one persistent launch per
+    SIRT phase over all instances, captured in a CUDA graph with FLAG_GRAPH."""
+
+    def __init__(self, ctx: Context, instances: Sequence[tuple], p: Params, mem_kind=MEM_HOST):
+        self.ctx, self.p = ctx, p
+        self.vols = [vol for _, vol in instances]
+        keep = []
+        arr = (InstanceC * len(instances))()
+        for i, (axes, vol) in enumerate(instances):
+            ax = (AxisC * len(axes))(*[a.c_struct() for a in axes])
+            keep.append(ax)
+            arr[i] = InstanceC(len(axes), ax, vol)
+        h = _P()
+        ctx.check(ctx.lib.mtr_batch_create(ctx.h, len(instances), arr, C.byref(p), mem_kind, C.byref(h)),
+                  "mtr_batch_create")
+        self.h = h
+
+    def run(self) -> None:
+        self.ctx.check(self.ctx.lib.mtr_batch_run(self.h), "mtr_batch_run")
+
+    def download(self, i: int, out=None, mem_kind=MEM_HOST):
+        if out is None:
+            out = np.empty(self.vols[i].shape, np.float32)
+        self.ctx.check(self.ctx.lib.mtr_batch_download(self.h, i, _ptr(out), mem_kind), "mtr_batch_download")
+        return out
+
+    def info(self) -> dict:
+        vu, by = C.c_longlong(), C.c_longlong()
+        items = (C.c_longlong * 5)()
+        self.ctx.check(self.ctx.lib.mtr_batch_info(self.h, C.byref(vu), C.byref(by), items), "mtr_batch_info")
+        return {"voxel_updates": vu.value, "bytes": by.value,
+                "items": dict(zip(["forward", "residual", "backproject", "mace", "fallback_axes"], list(items)))}
+
+    def close(self) -> None:
+        if self.h:
+            self.ctx.lib.mtr_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

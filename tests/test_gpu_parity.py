@@ -177,6 +177,37 @@ def test_windowed_and_plain_kernels_agree(ctx, monkeypatch):
     assert rel_l2(tma, plain) < 1e-5
 
 
+# --- autotuned tile shapes: every depth variant is correct, the cache persists -------
+
+@pytest.mark.parametrize("depths", ["4,8,0,0", "8,16,1,1", "16,32,0,1", "16,8,1,0", "8,32"])
+@pytest.mark.parametrize("name", ["mid", "mid_oblique"])
+def test_every_brick_depth_matches_oracle(ctx, monkeypatch, name, depths):
+    monkeypatch.setenv("MTR_FORCE_DEPTHS", depths)
+    c = cases.get(name)
+    p = mtr.params(iter_times=1, sirt_inner=3, sirt_step=0.5, mace_step=0.7)
+    got = ctx.reconstruct(c.axes, c.vol, p)
+    want = oracle.reconstruct(oracle.REF_FAITHFUL, c.axes, c.vol, 1, 3, 0.5, 0.7)
+    assert rel_l2(got, want) < FP32_TOL
+
+
+def test_autotune_cache_file(ctx, monkeypatch, tmp_path):
+    import json
+
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("MTR_AUTOTUNE_CACHE", str(cache))
+    c = cases.get("mid")
+    # a geometry not seen before in this process: shift the volume frame
+    v = mtr.VolumeSize.make(c.vol.Xstart, c.vol.Xend, c.vol.Ystart, c.vol.Yend, 0, 19)
+    p = mtr.params(iter_times=1, sirt_inner=2, sirt_step=0.5, mace_step=0.7)
+    ctx.reconstruct(c.axes, v, p)
+    d = json.loads(cache.read_text())
+    # lane -1: no windowed candidate fits that detector (the plain kernel runs)
+    assert d and all(b in (4, 8, 16) and f in (8, 16, 32) and bl in (-1, 0, 1) and fl in (-1, 0, 1)
+                     for b, f, bl, fl in d.values())
+    key = next(k for k in d if k.startswith("p72x72x13_v64x48x19"))
+    assert d[key][2] in (0, 1) and d[key][3] in (0, 1)  # this detector fits both windowed kernels
+
+
 # --- the all-FP64 GPU path used as the error reference at full sizes ---------------
 
 @pytest.mark.parametrize("name", ["two_axis", "mid_oblique", "rect"])

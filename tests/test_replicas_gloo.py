@@ -1,0 +1,65 @@
+"""Multi-GPU runs of the benchmark are independent replicas (one process per
+GPU, no collective on the data path).  This checks the host-side pieces of
+that path on CPU with two gloo ranks: the max-over-ranks timing and the
+whole-job aggregation, and that a non-zero rank of the reference arm exits
+without work."""
+import os
+import socket
+import subprocess
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _free_port() -> int:
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    p = s.getsockname()[1]
+    s.close()
+    return p
+
+
+def _worker(rank: int, world: int, port: int, q):
+    import torch.distributed as dist
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms = 100.0 + 50.0 * rank  # rank 1 is the slowest
+    mx = bench.reduce_max(ms)
+    value = bench.replica_value(1_000_000, world, mx)
+    dist.barrier()
+    dist.destroy_process_group()
+    q.put((rank, mx, value))
+
+
+def test_two_rank_aggregation():
+    import multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=120)
+    assert all(p.exitcode == 0 for p in procs)
+    res = sorted(q.get(timeout=5) for _ in range(2))
+    for rank, mx, value in res:
+        assert mx == pytest.approx(150.0)
+        assert value == pytest.approx(2 * 1_000_000 / 0.150)
+
+
+def test_reference_arm_nonzero_rank_exits_without_work():
+    env = dict(os.environ, RANK="1", WORLD_SIZE="2", LOCAL_RANK="1")
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference"], env=env,
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0
+    assert r.stdout.strip() == ""
