@@ -51,6 +51,22 @@ CONFIGS = {
 }
 
 
+# Per-launch DRAM traffic and instruction count of the dominant kernel, from
+# the ncu captures summarised in profiles/ (one launch of axis 0).
+NCU_PROFILES = {
+    ("c2", "backproject"): {"traffic": 330_938_368 + 157_545_984, "warp_inst_per_voxel_angle": 1_426_398_948 /
+                            (512 * 512 * 128 * 61), "sms": 152,
+                            "source": "profiles/bp_tma_kernel_3axis_512x512x128.md"},
+}
+
+
+def cfg_voxel_angles(cfg: dict) -> int:
+    """Voxel-angle evaluations of one projector launch (one axis, all angles)."""
+    x0, x1, y0, y1, z0, z1 = cfg["vol"]
+    t0, t1, dt = cfg["tilts"]
+    return (x1 - x0) * (y1 - y0) * (z1 - z0) * len(range(t0, t1, dt))
+
+
 def peaks() -> tuple[dict, str]:
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -282,12 +298,25 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
             arr_ms.append(dt * 1e3)
     e2e_ms = max_over_ranks(statistics.mean(arr_ms))
 
+    # error of both paths against the all-FP64 GPU reconstruction of the same inputs
+    err64 = None
+    if args.fp64 and args.config != "c3":
+        rec.close()
+        if ref32 is not rec:
+            ref32.close()
+        t = time.time()
+        out64 = ctx.reconstruct_fp64(host_axes, vol, mk(mtr.PREC_FP32))
+        n64 = max(float(np.linalg.norm(out64)), 1e-300)
+        err64 = {"mixed_vs_fp64_rel_l2": float(np.linalg.norm(out_mixed - out64) / n64),
+                 "fp32_vs_fp64_rel_l2": float(np.linalg.norm(out_fp32 - out64) / n64),
+                 "fp64_run_s": round(time.time() - t, 1)}
+
     vu = voxel_updates(cfg)
     res = {"tiles": tiles, "ms": ms, "ms32": ms32, "e2e_ms": e2e_ms, "h2d": h2d, "d2h": vol.X * vol.Y * vol.Z * 4, "clk": clk,
            "prof": prof, "launches": launches, "gen_s": gen_s, "meta": meta, "vu": vu,
            "mixed_vs_fp32": float(np.linalg.norm(out_mixed.astype(np.float64) - out_fp32) /
                                   max(np.linalg.norm(out_fp32.astype(np.float64)), 1e-30)),
-           "axes_host": host_axes, "vol": vol, "prec": prec}
+           "axes_host": host_axes, "vol": vol, "prec": prec, "err64": err64}
     rec.close()
     if ref32 is not rec:
         ref32.close()
@@ -301,16 +330,18 @@ C4 = dict(workload="64 seeded tilt series, detector and volume lateral size U{12
           n=64, seed=1004, n_ell=8, n_outer=1, n_inner=3)
 
 
-def make_batch_instances(device: str):
-    """The 64 uneven instances (host float32 projections; generated on the GPU)."""
+def make_batch_instances(device: str, n: int | None = None, seed: int | None = None):
+    """Uneven instances of the batched workload's size distribution (host
+    float32 projections; generated on the GPU)."""
     import torch
 
     import mtr
     import phantom
 
-    rng = np.random.default_rng(C4["seed"])
+    seed = C4["seed"] if seed is None else seed
+    rng = np.random.default_rng(seed)
     inst = []
-    for i in range(C4["n"]):
+    for i in range(C4["n"] if n is None else n):
         px = int(rng.integers(128, 1025))
         A = int(rng.integers(41, 122))
         K = int(rng.integers(1, 5))
@@ -318,7 +349,7 @@ def make_batch_instances(device: str):
         vol = mtr.VolumeSize.make(0, px, 0, px, 0, Z)
         tilts = np.linspace(-60.0, 60.0, A)
         phis = [k * 180.0 / K for k in range(K)]
-        case = phantom.make_case_torch(vol, px, tilts, phis, C4["n_ell"], "gaussian", 0.02, C4["seed"] * 100 + i,
+        case = phantom.make_case_torch(vol, px, tilts, phis, C4["n_ell"], "gaussian", 0.02, seed * 100 + i,
                                        device=device)
         axes = [mtr.AxisData(xc, yc, d.cpu().numpy()) for (xc, yc, d) in case["axes"]]
         del case
@@ -356,13 +387,30 @@ def run_batch_bench(args) -> dict:
     launches = (ctx.launch_count() - launches0) // max(1, args.steps)
     batched = [batch.download(i) for i in range(len(inst))]
     batch.close()
+    # per-phase device time of one run, without the graph (events around each launch)
+    pn = mtr.params(iter_times=C4["n_outer"], sirt_inner=C4["n_inner"], sirt_step=0.5, mace_step=0.7, precision=prec)
+    batch = mtr.Batch(ctx, inst, pn)
+    batch.run()
+    torch.cuda.synchronize()
+    ctx.profile_reset()
+    ctx.set_profiling(True)
+    batch.run()
+    torch.cuda.synchronize()
+    ctx.set_profiling(False)
+    batch_prof = {k: round(v[1], 2) for k, v in ctx.profile().items()}
+    batch.close()
     # plain FP32 path looped over the instances (device-resident inputs, run only timed)
     pf = mtr.params(iter_times=C4["n_outer"], sirt_inner=C4["n_inner"], sirt_step=0.5, mace_step=0.7)
     loop_ms, errs = 0.0, []
+    ctx.profile_reset()
     for i, (axes, vol) in enumerate(inst):
         r = mtr.Recon(ctx, axes, vol, pf)
         r.run()  # warm-up (module load, first-touch)
         loop_ms += time_steps(torch, stream, r, 1)
+        ctx.set_profiling(True)
+        r.run()
+        torch.cuda.synchronize()
+        ctx.set_profiling(False)
         ref = r.download()
         r.close()
         errs.append(float(np.linalg.norm(batched[i] - ref) / max(np.linalg.norm(ref), 1e-30)))
@@ -377,10 +425,102 @@ def run_batch_bench(args) -> dict:
                        "lateral_px": [min(sizes), max(sizes)], "seed": C4["seed"],
                        "l2": "inputs larger than L2", "generation_s": round(gen_s, 1),
                        "create_and_tune_s": round(create_s, 1)},
+            "phase_ms": {"batched": batch_prof, "fp32_loop": {k: round(v[1], 2) for k, v in ctx.profile().items()}},
             "fp32_loop": {"value": vu / (loop_ms * 1e-3), "ms_per_step": loop_ms,
                           "batched_over_loop": loop_ms / ms,
                           "rel_l2_batched_vs_fp32_max": max(errs), "rel_l2_batched_vs_fp32_median": float(np.median(errs))},
             "gpu_launches": launches, "e2e": None}
+
+
+C5 = dict(workload="serving: Poisson arrivals of reconstruction requests drawn from a pool of 12 seeded instances "
+                   "of the batched workload's size distribution (lateral U{128..1024} px, tilts U{41..121}, axes "
+                   "U{1..4}, depth U{32..256}); each request 1..3 MACE x 10 SIRT (10-30 iterations), lambda 0.5, "
+                   "rho 0.7; admission by device footprint under a 180 GB budget; continuous batching",
+          pool=12, seed=1005, budget=180 * 10**9, rates=(0.5, 1, 2, 5, 10, 50), per_rate=12)
+
+
+def serve_rate(mtr, ctx, pool, rate: float, n_req: int, precision: int, rng, keep: int = 0) -> dict:
+    """Serve n_req Poisson arrivals at `rate` req/s; latency = retire time - arrival time."""
+    srv = mtr.Server(ctx, C5["budget"], precision)
+    gaps = rng.exponential(1.0 / rate, n_req)
+    arrive = np.cumsum(gaps) - gaps[0]
+    picks = rng.integers(0, len(pool), n_req)
+    outer = rng.integers(1, 4, n_req)
+    ids, lat, kept, vu = {}, {}, {}, 0
+    t0 = time.perf_counter()
+    nxt = 0
+    while len(lat) < n_req:
+        now = time.perf_counter() - t0
+        while nxt < n_req and arrive[nxt] <= now:
+            axes, vol = pool[picks[nxt]]
+            ids[srv.submit(axes, vol, int(outer[nxt]), 10, 0.5, 0.7)] = nxt
+            vu += vol.X * vol.Y * vol.Z * len(axes) * int(outer[nxt]) * 10
+            nxt += 1
+        st = srv.stats()
+        if st["queued"] == 0 and st["active"] == 0 and nxt < n_req:
+            time.sleep(max(0.0, arrive[nxt] - (time.perf_counter() - t0)))
+            continue
+        for rid, v in srv.step():
+            i = ids[rid]
+            lat[i] = time.perf_counter() - t0 - arrive[i]
+            if i < keep:
+                kept[i] = v
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    ls = np.array([lat[i] for i in range(n_req)]) * 1e3
+    return {"rate_req_s": rate, "requests": n_req, "p50_ms": float(np.percentile(ls, 50)),
+            "p99_ms": float(np.percentile(ls, 99)), "throughput_req_s": n_req / wall,
+            "voxel_updates_per_s": vu / wall, "steps": st["steps"], "peak_bytes": st["peak_bytes"],
+            "wall_s": wall, "_kept": kept, "_picks": picks[:keep].tolist(), "_outer": outer[:keep].tolist()}
+
+
+def run_serve_bench(args) -> dict:
+    """Config 5: rate sweep of the continuous-batching server, mixed (BF16
+    storage) and FP32; the first requests of the lowest rate are compared
+    between the two precisions."""
+    import torch
+
+    import mtr
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = mtr.Context(0)
+    ctx.set_stream(stream.cuda_stream)
+    t0 = time.time()
+    pool = make_batch_instances("cuda:0", n=C5["pool"], seed=C5["seed"])
+    gen_s = time.time() - t0
+    torch.cuda.empty_cache()
+    prec = {"bf16": mtr.PREC_MIXED_BF16, "fp16": mtr.PREC_MIXED_FP16, "fp32": mtr.PREC_FP32}[args.precision]
+    # warm-up: every pool member once (tile tuning, module load)
+    for p in (prec, mtr.PREC_FP32):
+        srv = mtr.Server(ctx, C5["budget"], p)
+        for axes, vol in pool:
+            srv.submit(axes, vol, 1, 1)
+        srv.drain()
+        srv.close()
+    rates = C5["rates"]
+    out = {}
+    for name, p in ((args.precision, prec), ("fp32", mtr.PREC_FP32)):
+        rng = np.random.default_rng(C5["seed"])
+        out[name] = [serve_rate(mtr, ctx, pool, r, C5["per_rate"], p, rng, keep=4 if r == rates[0] else 0)
+                     for r in rates]
+    a, b = out[args.precision][0]["_kept"], out["fp32"][0]["_kept"]
+    errs = [float(np.linalg.norm(a[i] - b[i]) / max(np.linalg.norm(b[i]), 1e-30)) for i in sorted(a)]
+    for rows in out.values():
+        for r in rows:
+            for k in ("_kept", "_picks", "_outer"):
+                r.pop(k)
+    top = out[args.precision][-1]
+    return {"metric": METRIC, "value": top["voxel_updates_per_s"], "unit": UNIT, "n_gpus": 1, "steps": len(rates),
+            "warmup": 1, "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": C5["workload"], "precision": args.precision, "budget_bytes": C5["budget"],
+                       "rates_req_s": list(rates), "requests_per_rate": C5["per_rate"], "seed": C5["seed"],
+                       "pool_generation_s": round(gen_s, 1), "value_at": f"{rates[-1]} req/s (saturated)"},
+            "serve": out, "error": {"mixed_vs_fp32_rel_l2_max": max(errs), "requests_compared": len(errs)},
+            "gpu_launches": None, "e2e": None}
 
 
 def cpu_baseline(cfg: dict, vol, axes_host, budget_s: float = 20.0) -> dict:
@@ -446,11 +586,12 @@ def main() -> int:
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c4"])
+    ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c4", "c5"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64", type=int, default=1, help="1: state both paths' error against the FP64 GPU run")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
@@ -465,9 +606,10 @@ def main() -> int:
 
     import __graft_entry__
 
-    if args.config == "c4":
+    if args.config in ("c4", "c5"):
         __graft_entry__.build()
-        print(json.dumps(run_batch_bench(args)), flush=True)
+        line = run_batch_bench(args) if args.config == "c4" else run_serve_bench(args)
+        print(json.dumps(line), flush=True)
         return 0
 
     if rank == 0 or world == 1:
@@ -492,11 +634,23 @@ def main() -> int:
         per_launch_ms = tot / n_l
         alg, alg_desc = algorithmic_bytes(dom, cfg, r["prec"])
         achieved = alg / (per_launch_ms * 1e-3) / 1e9
+        ncu = NCU_PROFILES.get((args.config, dom))
         roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
-                "frac": achieved / pk["hbm_gbs"], "traffic": None, "kernel": dom, "peak_source": pk_kind,
+                "frac": achieved / pk["hbm_gbs"], "traffic": ncu["traffic"] if ncu else None, "kernel": dom,
+                "peak_source": pk_kind,
                 "algorithmic_bytes_per_launch": alg, "algorithmic_bytes": alg_desc,
                 "avg_launch_ms": per_launch_ms, "launches": n_l,
                 "kernel_share": {k: prof[k][1] / max(sum(x[1] for x in prof.values()), 1e-9) for k in prof}}
+        if ncu:
+            # the roof that binds: instruction issue (ncu instruction count per
+            # voxel-angle x live launch rate, against 4 issue slots per SM per clock)
+            va = cfg_voxel_angles(cfg)
+            issue_peak = ncu["sms"] * 4 * (r["clk"]["sm_mhz"] or 2070.0) * 1e6
+            inst_rate = ncu["warp_inst_per_voxel_angle"] * va / (per_launch_ms * 1e-3)
+            roof["binding"] = {"resource": "instruction issue", "achieved": inst_rate, "peak": issue_peak,
+                               "unit": "warp-instructions/s", "frac": inst_rate / issue_peak,
+                               "warp_inst_per_voxel_angle": ncu["warp_inst_per_voxel_angle"],
+                               "source": ncu["source"]}
         vu = r["vu"] * world
         value = replica_value(r["vu"], world, r["ms"])
         line = {
@@ -513,7 +667,7 @@ def main() -> int:
                                   "tma": t["back_projection"]["tma"] and t["forward"]["tma"]} for t in r["tiles"]]},
             "fp32": {"value": vu / (r["ms32"] * 1e-3), "ms_per_step": r["ms32"],
                      "mixed_over_fp32": r["ms32"] / r["ms"]},
-            "error": {"mixed_vs_fp32_rel_l2": r["mixed_vs_fp32"]},
+            "error": {"mixed_vs_fp32_rel_l2": r["mixed_vs_fp32"], **(r["err64"] or {})},
             "e2e": {"value": vu / (r["e2e_ms"] * 1e-3), "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"],
                     "api": "mtr_reconstruct (host buffers, pinned)"},

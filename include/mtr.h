@@ -252,6 +252,51 @@ mtr_status mtr_batch_info(const mtr_batch* b, long long* voxel_updates_per_run, 
                           long long* work_items5);
 mtr_status mtr_batch_destroy(mtr_batch* b);
 
+/* ---- Serving: continuous batching with admission by device footprint -----
+ * No counterpart in the reference (MultiAxis.cpp runs one reconstruction per
+ * process); this is the serving entry the batch layer feeds.
+ *
+ * Requests are queued by mtr_server_submit and admitted in arrival order
+ * while the sum of admitted footprints (mtr_estimate_footprint) stays within
+ * the server's byte budget.  Each mtr_server_step:
+ *   1. waits for the previous step's GPU work,
+ *   2. retires requests whose last MACE step has run: copies the consensus
+ *      volume to the request's `out` buffer, frees its device memory and
+ *      reports its id,
+ *   3. admits queued requests that fit (device buffers, projection upload,
+ *      tile tuning, WBP init),
+ *   4. enqueues one SIRT iteration of every admitted request as one
+ *      persistent launch per phase (forward, residual, back-projection),
+ *      then the MACE step of each request that finished an outer iteration.
+ * A request's `axes[].data` and `out` must stay valid until its id is
+ * reported.  All requests of a server share one precision. */
+typedef struct mtr_request {
+  int n_axes;
+  const mtr_axis* axes;   /* host projections */
+  mtr_volume_size vol;
+  int iter_times;         /* MACE outer iterations */
+  int sirt_inner;         /* SIRT iterations per outer iteration */
+  float sirt_step;
+  float mace_step;
+  float* out;             /* host, X*Y*Z floats: the consensus volume */
+} mtr_request;
+typedef struct mtr_server_stats {
+  long long submitted, completed;
+  long long queued, active;        /* now */
+  long long bytes_in_use, peak_bytes, budget_bytes;
+  long long steps;                 /* mtr_server_step calls that enqueued work */
+  long long voxel_updates;         /* of completed requests */
+} mtr_server_stats;
+typedef struct mtr_server mtr_server;
+mtr_status mtr_server_create(mtr_context* ctx, long long budget_bytes, int precision, mtr_server** out);
+/* MTR_ERR_CAPACITY if the request alone exceeds the budget. */
+mtr_status mtr_server_submit(mtr_server* s, const mtr_request* req, long long* id);
+/* One scheduling step (see above); writes up to max_done retired ids. */
+mtr_status mtr_server_step(mtr_server* s, int max_done, long long* done_ids, int* n_done);
+mtr_status mtr_server_stats_get(const mtr_server* s, mtr_server_stats* st);
+/* Waits for outstanding GPU work; queued and active requests are dropped. */
+mtr_status mtr_server_destroy(mtr_server* s);
+
 /* ---- MRC / TXBR / options (the reference's file I/O boundary) ----------- */
 
 /* 1024-byte MRC header, same layout as MrcHeader (MrcFileIOBaseFunction.h:99-173). */

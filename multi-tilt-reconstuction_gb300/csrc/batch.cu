@@ -2,17 +2,22 @@
 //
 // Each instance is an mtr_recon (its own buffers, WBP init and MACE state).
 // The SIRT phases of all instances run together: per phase ONE persistent
-// launch whose CTAs (a grid sized to the GPU's resident capacity) loop over a
-// cost-ordered work list covering every instance and axis:
-//   forward splat   item = (axis, brick)          fwd_batch_kernel
-//   residual        item = (axis, 64 Ki pixels)   residual_batch_kernel
-//   back-projection item = (axis, brick)          bp_batch_kernel
+// launch whose CTAs (a grid sized to the GPU's resident capacity) take the
+// items of a work list covering every instance and axis:
+//   forward splat   item = (axis, brick)            fwd_batch_kernel
+//   residual        item = (axis, 64 Ki pixels)     residual_batch_kernel
+//   back-projection item = (axis, brick)            bp_batch_kernel
 //   MACE consensus  item = (instance, 64 Ki voxels) mace_batch_kernel
-// so small instances no longer leave SMs idle.  The whole schedule (WBP init
-// of every instance, n_outer x n_inner SIRT phases, MACE steps) is captured
-// once into a CUDA graph and replayed.  An axis whose detector window does
-// not fit a TMA box falls back to its own plain kernels inside the same
-// phase.  Work lists and tensor maps live in device memory, built once.
+// so small instances no longer leave SMs idle.  An axis with enough bricks to
+// fill the GPU for kOwnWaves waves keeps its own single launch instead (its
+// brick arguments then sit in the constant bank, which the persistent kernels
+// have to stage through shared memory).  A work list is a descriptor
+// table in cost order plus the prefix sum of the descriptors' item counts;
+// a CTA finds its descriptor by binary search.  Each axis keeps the brick
+// depth, lane axis and tensor maps it was tuned to.  The whole schedule (WBP
+// init of every instance, n_outer x n_inner SIRT phases, MACE steps) is
+// captured once into a CUDA graph and replayed.  An axis whose detector
+// window fits no TMA box runs its own plain kernels inside the same phase.
 #include <algorithm>
 #include <memory>
 #include <new>
@@ -24,17 +29,210 @@
 
 using namespace mtr;
 
+namespace {
+
+int copy_kind_of(int precision) {
+  return precision == MTR_PREC_MIXED_BF16 ? 1 : precision == MTR_PREC_MIXED_FP16 ? 2 : 0;
+}
+
+constexpr int kOwnWaves = 4;
+
+int forward_ctas_per_sm(int ck, size_t smem) {
+  if (ck == 1) return forward_batch_ctas_per_sm<__nv_bfloat16>(smem);
+  if (ck == 2) return forward_batch_ctas_per_sm<__half>(smem);
+  return forward_batch_ctas_per_sm<float>(smem);
+}
+
+// Copy a host table to a device buffer that only grows.
+template <typename T>
+mtr_status upload_grow(mtr_context* ctx, DevBuf& buf, const std::vector<T>& v) {
+  if (v.empty()) return MTR_OK;
+  const size_t n = sizeof(T) * v.size();
+  if (buf.bytes < n) MTR_CK(ctx, buf.alloc(n + n / 2));
+  MTR_CK(ctx, cudaMemcpyAsync(buf.p, v.data(), n, cudaMemcpyHostToDevice, ctx->stream));
+  return MTR_OK;
+}
+
+// Reorder descriptors by decreasing per-item cost; returns the prefix sum of
+// the item counts in the new order (n + 1 entries).
+template <typename D>
+std::vector<long long> order_by_cost(std::vector<D>& descs, const std::vector<long long>& counts,
+                                     const std::vector<long long>& cost) {
+  std::vector<int> idx(descs.size());
+  std::iota(idx.begin(), idx.end(), 0);
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<D> d2;
+  std::vector<long long> first(1, 0);
+  for (int i : idx) {
+    d2.push_back(descs[i]);
+    first.push_back(first.back() + counts[i]);
+  }
+  descs.swap(d2);
+  return first;
+}
+
+}  // namespace
+
+mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*>& recs, int precision,
+                                  SirtTables& t) {
+  const int ck = copy_kind_of(precision);
+  t.copy_kind = ck;
+  t.bp_own.clear();
+  t.fwd_own.clear();
+  t.bp_smem = t.fwd_smem = 0;
+  std::vector<CUtensorMap> maps;
+  std::vector<BpBatchDesc> bpd;
+  std::vector<FwdBatchDesc> fwd;
+  std::vector<ResBatchDesc> resd;
+  std::vector<long long> bp_count, fwd_count, res_count, bp_cost, fwd_cost, res_cost;
+  std::vector<int> bp_map, fwd_map;  // index of each descriptor's tensor map in `maps`
+  for (mtr_recon* r : recs) {
+    if (copy_kind_of(r->p.precision) != ck) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "mixed precisions");
+    const VolDev& v = r->vol;
+    for (int k = 0; k < r->K; ++k) {
+      AxisState& a = r->ax[k];
+      resd.push_back(ResBatchDesc{a.b.p, a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), a.np});
+      res_count.push_back((a.np + kBatchChunk - 1) / kBatchChunk);
+      res_cost.push_back(1);
+      // brick depth, lane axis, windows and tensor maps as tuned for this axis
+      const BpPlan& bp = a.plan;
+      const FwdPlan& fp = a.fplan;
+      const int bgx = (v.NX + (bp.lane_y ? 8 : 32) - 1) / (bp.lane_y ? 8 : 32);
+      const int bgy = (v.NY + (bp.lane_y ? 32 : 8) - 1) / (bp.lane_y ? 32 : 8);
+      const int fgx = (v.NX + (fp.lane_y ? 8 : 32) - 1) / (fp.lane_y ? 8 : 32);
+      const int fgy = (v.NY + (fp.lane_y ? 32 : 8) - 1) / (fp.lane_y ? 32 : 8);
+      const bool bp_ok = a.tma && !tma_disabled() &&
+                         (long long)bgx * bgy * ((v.NZ + bp.nz - 1) / bp.nz) <
+                             (long long)kOwnWaves * ctx->num_sms * backproject_batch_ctas_per_sm(bp.smem);
+      const bool fwd_ok = a.ftma && !tma_disabled() &&
+                          (long long)fgx * fgy * ((v.NZ + fp.nz - 1) / fp.nz) <
+                              (long long)kOwnWaves * ctx->num_sms * forward_ctas_per_sm(ck, fp.smem);
+      const int j = (int)maps.size() / 2;
+      maps.push_back(a.map_r);
+      maps.push_back(a.map_s);
+      if (bp_ok) {
+        BpBatchDesc d{};
+        d.ax = a.dev();
+        d.vol = v;
+        d.WX = bp.WX; d.WY = bp.WY; d.align = bp.align;
+        const int BX = bp.lane_y ? 8 : 32, BY = bp.lane_y ? 32 : 8;
+        d.gx = (v.NX + BX - 1) / BX;
+        d.gy = (v.NY + BY - 1) / BY;
+        d.lane_y = bp.lane_y; d.bz0 = bp.bz0; d.nz = bp.nz;
+        d.step = r->p.sirt_step;
+        d.vol_out = a.x.as<float>();
+        d.cbp = a.cbp.as<float>();
+        d.vol_copy = a.xcopy.p;
+        d.copy_kind = ck;
+        d.map = nullptr;  // set after the maps are uploaded
+        bpd.push_back(d);
+        bp_map.push_back(2 * j);
+        bp_count.push_back((long long)d.gx * d.gy * ((v.NZ + d.nz - 1) / d.nz));
+        bp_cost.push_back((long long)a.A * d.nz);
+        t.bp_smem = std::max(t.bp_smem, bp.smem);
+      } else {
+        t.bp_own.push_back({r, k});
+      }
+      if (fwd_ok) {
+        FwdBatchDesc d{};
+        d.ax = a.dev();
+        d.vol = v;
+        d.WX = fp.WX; d.WY = fp.WY; d.mass_shift = fp.mass_shift;
+        const int BX = fp.lane_y ? 8 : 32, BY = fp.lane_y ? 32 : 8;
+        d.gx = (v.NX + BX - 1) / BX;
+        d.gy = (v.NY + BY - 1) / BY;
+        d.lane_y = fp.lane_y; d.bz0 = fp.bz0; d.nz = fp.nz;
+        d.x = ck ? a.xcopy.p : a.x.p;
+        d.map = nullptr;
+        fwd.push_back(d);
+        fwd_map.push_back(2 * j + 1);
+        fwd_count.push_back((long long)d.gx * d.gy * ((v.NZ + d.nz - 1) / d.nz));
+        fwd_cost.push_back((long long)a.A * d.nz);
+        t.fwd_smem = std::max(t.fwd_smem, fp.smem);
+      } else {
+        t.fwd_own.push_back({r, k});
+      }
+    }
+  }
+  mtr_status s = upload_grow(ctx, t.maps, maps);
+  if (s != MTR_OK) return s;
+  const CUtensorMap* base = t.maps.as<CUtensorMap>();
+  for (size_t q = 0; q < bpd.size(); ++q) bpd[q].map = base + bp_map[q];
+  for (size_t q = 0; q < fwd.size(); ++q) fwd[q].map = base + fwd_map[q];
+  const std::vector<long long> bpf = order_by_cost(bpd, bp_count, bp_cost);
+  const std::vector<long long> fwf = order_by_cost(fwd, fwd_count, fwd_cost);
+  const std::vector<long long> ref = order_by_cost(resd, res_count, res_cost);
+  t.n_bp_desc = (int)bpd.size();
+  t.n_fwd_desc = (int)fwd.size();
+  t.n_res_desc = (int)resd.size();
+  t.n_bp = bpf.back();
+  t.n_fwd = fwf.back();
+  t.n_res = ref.back();
+  if ((s = upload_grow(ctx, t.bp_descs, bpd)) != MTR_OK || (s = upload_grow(ctx, t.fwd_descs, fwd)) != MTR_OK ||
+      (s = upload_grow(ctx, t.res_descs, resd)) != MTR_OK || (s = upload_grow(ctx, t.bp_first, bpf)) != MTR_OK ||
+      (s = upload_grow(ctx, t.fwd_first, fwf)) != MTR_OK || (s = upload_grow(ctx, t.res_first, ref)) != MTR_OK)
+    return s;
+  const int sms = ctx->num_sms;
+  t.bp_grid = t.n_bp ? (int)std::min<long long>(t.n_bp, (long long)sms * backproject_batch_ctas_per_sm(t.bp_smem)) : 0;
+  t.fwd_grid = t.n_fwd ? (int)std::min<long long>(t.n_fwd, (long long)sms * forward_ctas_per_sm(ck, t.fwd_smem)) : 0;
+  t.ew_grid = sms * 8;
+  // the host tables are released on return: wait for their copies
+  MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  return MTR_OK;
+}
+
+mtr_status mtr::enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, int* err) {
+  cudaStream_t st = ctx->stream;
+  {
+    ProfScope ps(ctx, MTR_KERNEL_FORWARD);
+    if (t.n_fwd > 0) {
+      const FwdBatchDesc* d = t.fwd_descs.as<FwdBatchDesc>();
+      const long long* f = t.fwd_first.as<long long>();
+      cudaError_t e;
+      if (t.copy_kind == 1)
+        e = launch_forward_batch<__nv_bfloat16>(d, f, t.n_fwd_desc, t.n_fwd, t.fwd_smem, t.fwd_grid, st);
+      else if (t.copy_kind == 2)
+        e = launch_forward_batch<__half>(d, f, t.n_fwd_desc, t.n_fwd, t.fwd_smem, t.fwd_grid, st);
+      else
+        e = launch_forward_batch<float>(d, f, t.n_fwd_desc, t.n_fwd, t.fwd_smem, t.fwd_grid, st);
+      g_launches.fetch_add(1);
+      if (e != cudaSuccess) return cuda_error(ctx, e, "batched forward");
+    }
+  }
+  for (auto& f : t.fwd_own) {
+    mtr_status s = recon_enqueue_forward(f.first, f.second);
+    if (s != MTR_OK) return s;
+  }
+  if (t.n_res > 0) {
+    ProfScope ps(ctx, MTR_KERNEL_RESIDUAL);
+    launch_residual_batch(t.res_descs.as<ResBatchDesc>(), t.res_first.as<long long>(), t.n_res_desc, t.n_res,
+                          t.copy_kind != 0, t.ew_grid, st);
+    MTR_CK_LAUNCH(ctx, "batched residual");
+  }
+  {
+    ProfScope ps(ctx, MTR_KERNEL_BACKPROJECT);
+    if (t.n_bp > 0) {
+      cudaError_t e = launch_backproject_batch(t.bp_descs.as<BpBatchDesc>(), t.bp_first.as<long long>(), t.n_bp_desc,
+                                               t.n_bp, t.bp_smem, t.bp_grid, err, st);
+      g_launches.fetch_add(1);
+      if (e != cudaSuccess) return cuda_error(ctx, e, "batched back-projection");
+    }
+  }
+  for (auto& f : t.bp_own) {
+    mtr_status s = recon_enqueue_sirt_bp(f.first, f.second);
+    if (s != MTR_OK) return s;
+  }
+  return MTR_OK;
+}
+
 struct mtr_batch {
   mtr_context* ctx = nullptr;
   mtr_params p{};
   std::vector<mtr_recon*> rec;
-  DevBuf maps;  // CUtensorMap per batched axis: [2j] residual (bp), [2j+1] ray sums (fwd)
-  DevBuf bp_descs, fwd_descs, res_descs, mace_descs;
-  DevBuf bp_items, fwd_items, res_items, mace_items;
-  long long n_bp = 0, n_fwd = 0, n_res = 0, n_mace = 0;
-  size_t bp_smem = 0, fwd_smem = 0;
-  int bp_grid = 0, fwd_grid = 0, ew_grid = 0;
-  std::vector<std::pair<int, int>> bp_fallback, fwd_fallback;  // (instance, axis) run with their own kernels
+  SirtTables sirt;
+  DevBuf mace_descs, mace_first;
+  int n_mace_desc = 0;
+  long long n_mace = 0;
   DevBuf err;
   cudaGraphExec_t graph = nullptr;
   long long graph_nodes = 0;
@@ -47,141 +245,33 @@ struct mtr_batch {
 
 namespace {
 
-int copy_kind_of(int precision) {
-  return precision == MTR_PREC_MIXED_BF16 ? 1 : precision == MTR_PREC_MIXED_FP16 ? 2 : 0;
-}
-
-template <typename T>
-mtr_status upload(mtr_context* ctx, DevBuf& buf, const std::vector<T>& v) {
-  if (v.empty()) return MTR_OK;
-  MTR_CK(ctx, buf.alloc(sizeof(T) * v.size()));
-  MTR_CK(ctx, cudaMemcpyAsync(buf.p, v.data(), sizeof(T) * v.size(), cudaMemcpyHostToDevice, ctx->stream));
-  return MTR_OK;
-}
-
-// Items of all axes, ordered by decreasing per-item cost (angle count).
-std::vector<int2> order_items(const std::vector<long long>& counts, const std::vector<int>& cost) {
-  std::vector<int> idx(counts.size());
-  std::iota(idx.begin(), idx.end(), 0);
-  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
-  std::vector<int2> items;
-  for (int d : idx)
-    for (long long i = 0; i < counts[d]; ++i) items.push_back(make_int2(d, (int)i));
-  return items;
-}
-
-mtr_status build_work(mtr_batch* b) {
+mtr_status build_mace_table(mtr_batch* b) {
   mtr_context* ctx = b->ctx;
   const int ck = copy_kind_of(b->p.precision);
-  std::vector<CUtensorMap> maps;
-  std::vector<BpBatchDesc> bpd;
-  std::vector<FwdBatchDesc> fwd;
-  std::vector<ResBatchDesc> resd;
   std::vector<MaceBatchDesc> maced;
-  std::vector<long long> bp_count, fwd_count, res_count, mace_count;
-  std::vector<int> bp_cost, fwd_cost, res_cost, mace_cost;
-  std::vector<int> bp_map, fwd_map;  // index of each descriptor's tensor map in `maps`
-  for (size_t i = 0; i < b->rec.size(); ++i) {
-    mtr_recon* r = b->rec[i];
-    const VolDev& v = r->vol;
+  std::vector<long long> count, cost;
+  for (mtr_recon* r : b->rec) {
     MaceBatchDesc md{};
     md.K = r->K;
     for (int k = 0; k < r->K; ++k) {
-      AxisState& a = r->ax[k];
-      md.w[k] = a.w.as<float>();
-      md.x[k] = a.x.as<float>();
-      md.xc[k] = a.xcopy.p;
-      resd.push_back(ResBatchDesc{a.b.p, a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), a.np});
-      res_count.push_back((a.np + kBatchChunk - 1) / kBatchChunk);
-      res_cost.push_back(1);
-      // back-projection at the batch depth, lane axis as tuned for this axis
-      const int bp_lane = a.tma ? (a.plan.lane_y ? 1 : 0) : -1;
-      BpPlan bp = plan_backproject(a.hxc, a.hyc, a.A, false, kBatchBpNZ, bp_lane);
-      CUtensorMap mr{}, ms{};
-      const bool bp_ok = !tma_disabled() && bp.ok &&
-                         encode_tensor_map_3d(&mr, a.r.p, false, a.PX, a.pitch, a.PY, a.A, bp.WX, bp.WY);
-      const int fwd_lane = a.ftma ? (a.fplan.lane_y ? 1 : 0) : -1;
-      FwdPlan fp = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, kBatchFwdNZ, fwd_lane);
-      const bool fwd_ok = !tma_disabled() && fp.ok && fp.nz == kBatchFwdNZ &&
-                          encode_tensor_map_3d(&ms, a.s.p, false, a.pitch, a.pitch, a.PY, a.A, fp.WX, fp.WY);
-      const int j = (int)maps.size() / 2;
-      maps.push_back(mr);
-      maps.push_back(ms);
-      if (bp_ok) {
-        BpBatchDesc d{};
-        d.ax = a.dev();
-        d.vol = v;
-        d.WX = bp.WX; d.WY = bp.WY; d.align = bp.align;
-        const int BX = bp.lane_y ? 8 : 32, BY = bp.lane_y ? 32 : 8;
-        d.gx = (v.NX + BX - 1) / BX;
-        d.gy = (v.NY + BY - 1) / BY;
-        d.lane_y = bp.lane_y; d.bz0 = bp.bz0;
-        d.step = b->p.sirt_step;
-        d.vol_out = a.x.as<float>();
-        d.cbp = a.cbp.as<float>();
-        d.vol_copy = a.xcopy.p;
-        d.copy_kind = ck;
-        d.map = nullptr;  // set after the maps are uploaded
-        bpd.push_back(d);
-        bp_map.push_back(2 * j);
-        bp_count.push_back((long long)d.gx * d.gy * ((v.NZ + kBatchBpNZ - 1) / kBatchBpNZ));
-        bp_cost.push_back(a.A);
-        b->bp_smem = std::max(b->bp_smem, bp.smem);
-      } else {
-        b->bp_fallback.push_back({(int)i, k});
-      }
-      if (fwd_ok) {
-        FwdBatchDesc d{};
-        d.ax = a.dev();
-        d.vol = v;
-        d.WX = fp.WX; d.WY = fp.WY; d.mass_shift = fp.mass_shift;
-        const int BX = fp.lane_y ? 8 : 32, BY = fp.lane_y ? 32 : 8;
-        d.gx = (v.NX + BX - 1) / BX;
-        d.gy = (v.NY + BY - 1) / BY;
-        d.lane_y = fp.lane_y; d.bz0 = fp.bz0;
-        d.x = ck ? a.xcopy.p : a.x.p;
-        d.map = nullptr;
-        fwd.push_back(d);
-        fwd_map.push_back(2 * j + 1);
-        fwd_count.push_back((long long)d.gx * d.gy * ((v.NZ + kBatchFwdNZ - 1) / kBatchFwdNZ));
-        fwd_cost.push_back(a.A);
-        b->fwd_smem = std::max(b->fwd_smem, fp.smem);
-      } else {
-        b->fwd_fallback.push_back({(int)i, k});
-      }
+      md.w[k] = r->ax[k].w.as<float>();
+      md.x[k] = r->ax[k].x.as<float>();
+      md.xc[k] = r->ax[k].xcopy.p;
     }
     md.wavg = r->wavg.as<float>();
     md.n = r->nv;
-    md.rho = b->p.mace_step;
+    md.rho = r->p.mace_step;
     md.copy_kind = ck;
     maced.push_back(md);
-    mace_count.push_back((r->nv + kBatchChunk - 1) / kBatchChunk);
-    mace_cost.push_back(r->K);
+    count.push_back((r->nv + kBatchChunk - 1) / kBatchChunk);
+    cost.push_back(r->K);
   }
-  mtr_status s = upload(ctx, b->maps, maps);
+  const std::vector<long long> first = order_by_cost(maced, count, cost);
+  b->n_mace_desc = (int)maced.size();
+  b->n_mace = first.back();
+  mtr_status s = upload_grow(ctx, b->mace_descs, maced);
+  if (s == MTR_OK) s = upload_grow(ctx, b->mace_first, first);
   if (s != MTR_OK) return s;
-  const CUtensorMap* base = b->maps.as<CUtensorMap>();
-  for (size_t q = 0; q < bpd.size(); ++q) bpd[q].map = base + bp_map[q];
-  for (size_t q = 0; q < fwd.size(); ++q) fwd[q].map = base + fwd_map[q];
-  const std::vector<int2> bpi = order_items(bp_count, bp_cost), fwi = order_items(fwd_count, fwd_cost);
-  const std::vector<int2> rei = order_items(res_count, res_cost), mai = order_items(mace_count, mace_cost);
-  b->n_bp = (long long)bpi.size();
-  b->n_fwd = (long long)fwi.size();
-  b->n_res = (long long)rei.size();
-  b->n_mace = (long long)mai.size();
-  if ((s = upload(ctx, b->bp_descs, bpd)) != MTR_OK || (s = upload(ctx, b->fwd_descs, fwd)) != MTR_OK ||
-      (s = upload(ctx, b->res_descs, resd)) != MTR_OK || (s = upload(ctx, b->mace_descs, maced)) != MTR_OK ||
-      (s = upload(ctx, b->bp_items, bpi)) != MTR_OK || (s = upload(ctx, b->fwd_items, fwi)) != MTR_OK ||
-      (s = upload(ctx, b->res_items, rei)) != MTR_OK || (s = upload(ctx, b->mace_items, mai)) != MTR_OK)
-    return s;
-  const int sms = ctx->num_sms;
-  b->bp_grid = (int)std::min<long long>(b->n_bp, (long long)sms * backproject_batch_ctas_per_sm(b->bp_smem));
-  int fwd_per_sm = 1;
-  if (ck == 1) fwd_per_sm = forward_batch_ctas_per_sm<__nv_bfloat16>(b->fwd_smem);
-  else if (ck == 2) fwd_per_sm = forward_batch_ctas_per_sm<__half>(b->fwd_smem);
-  else fwd_per_sm = forward_batch_ctas_per_sm<float>(b->fwd_smem);
-  b->fwd_grid = (int)std::min<long long>(b->n_fwd, (long long)sms * fwd_per_sm);
-  b->ew_grid = sms * 8;
   MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return MTR_OK;
 }
@@ -189,7 +279,6 @@ mtr_status build_work(mtr_batch* b) {
 mtr_status enqueue_batch(mtr_batch* b) {
   mtr_context* ctx = b->ctx;
   cudaStream_t st = ctx->stream;
-  const int ck = copy_kind_of(b->p.precision);
   MTR_CK(ctx, cudaMemsetAsync(b->err.p, 0, sizeof(int), st));
   for (mtr_recon* r : b->rec) {
     mtr_status s = recon_enqueue_init(r);
@@ -197,49 +286,12 @@ mtr_status enqueue_batch(mtr_batch* b) {
   }
   for (int it = 0; it < b->p.iter_times; ++it) {
     for (int j = 0; j < b->p.sirt_inner; ++j) {
-      {
-        ProfScope ps(ctx, MTR_KERNEL_FORWARD);
-        if (b->n_fwd > 0) {
-          cudaError_t e;
-          if (ck == 1)
-            e = launch_forward_batch<__nv_bfloat16>(b->fwd_descs.as<FwdBatchDesc>(), b->fwd_items.as<int2>(),
-                                                    b->n_fwd, b->fwd_smem, b->fwd_grid, st);
-          else if (ck == 2)
-            e = launch_forward_batch<__half>(b->fwd_descs.as<FwdBatchDesc>(), b->fwd_items.as<int2>(), b->n_fwd,
-                                             b->fwd_smem, b->fwd_grid, st);
-          else
-            e = launch_forward_batch<float>(b->fwd_descs.as<FwdBatchDesc>(), b->fwd_items.as<int2>(), b->n_fwd,
-                                            b->fwd_smem, b->fwd_grid, st);
-          g_launches.fetch_add(1);
-          if (e != cudaSuccess) return cuda_error(ctx, e, "batched forward");
-        }
-      }
-      for (auto& f : b->fwd_fallback) {
-        mtr_status s = recon_enqueue_forward(b->rec[f.first], f.second);
-        if (s != MTR_OK) return s;
-      }
-      {
-        ProfScope ps(ctx, MTR_KERNEL_RESIDUAL);
-        launch_residual_batch(b->res_descs.as<ResBatchDesc>(), b->res_items.as<int2>(), b->n_res, ck != 0,
-                              b->ew_grid, st);
-        MTR_CK_LAUNCH(ctx, "batched residual");
-      }
-      {
-        ProfScope ps(ctx, MTR_KERNEL_BACKPROJECT);
-        if (b->n_bp > 0) {
-          cudaError_t e = launch_backproject_batch(b->bp_descs.as<BpBatchDesc>(), b->bp_items.as<int2>(), b->n_bp,
-                                                   b->bp_smem, b->bp_grid, b->err.as<int>(), st);
-          g_launches.fetch_add(1);
-          if (e != cudaSuccess) return cuda_error(ctx, e, "batched back-projection");
-        }
-      }
-      for (auto& f : b->bp_fallback) {
-        mtr_status s = recon_enqueue_sirt_bp(b->rec[f.first], f.second);
-        if (s != MTR_OK) return s;
-      }
+      mtr_status s = enqueue_sirt_iteration(ctx, b->sirt, b->err.as<int>());
+      if (s != MTR_OK) return s;
     }
     ProfScope ps(ctx, MTR_KERNEL_MACE);
-    launch_mace_batch(b->mace_descs.as<MaceBatchDesc>(), b->mace_items.as<int2>(), b->n_mace, b->ew_grid, st);
+    launch_mace_batch(b->mace_descs.as<MaceBatchDesc>(), b->mace_first.as<long long>(), b->n_mace_desc, b->n_mace,
+                      ctx->num_sms * 8, st);
     MTR_CK_LAUNCH(ctx, "batched mace");
   }
   return MTR_OK;
@@ -268,7 +320,8 @@ mtr_status mtr_batch_create(mtr_context* ctx, int n, const mtr_instance* inst, c
     b->voxel_updates += r->nv * r->K * (long long)params->iter_times * params->sirt_inner;
   }
   MTR_CK(ctx, b->err.alloc(sizeof(int)));
-  mtr_status s = build_work(b.get());
+  mtr_status s = build_sirt_tables(ctx, b->rec, params->precision, b->sirt);
+  if (s == MTR_OK) s = build_mace_table(b.get());
   if (s != MTR_OK) return s;
   *out = b.release();
   return MTR_OK;
@@ -325,11 +378,11 @@ mtr_status mtr_batch_info(const mtr_batch* b, long long* voxel_updates_per_run, 
     *device_bytes = t;
   }
   if (work_items) {
-    work_items[0] = b->n_fwd;
-    work_items[1] = b->n_res;
-    work_items[2] = b->n_bp;
+    work_items[0] = b->sirt.n_fwd;
+    work_items[1] = b->sirt.n_res;
+    work_items[2] = b->sirt.n_bp;
     work_items[3] = b->n_mace;
-    work_items[4] = (long long)(b->fwd_fallback.size() + b->bp_fallback.size());
+    work_items[4] = (long long)(b->sirt.fwd_own.size() + b->sirt.bp_own.size());
   }
   return MTR_OK;
 }

@@ -281,12 +281,14 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   }
 }
 
-// One CTA per brick of one axis.
+// One CTA per brick of one axis.  The grid runs x fastest, then z, then y:
+// bricks of the same rows at all depths run together, so the detector rows
+// they read stay in L2 instead of being re-read from DRAM once per z layer.
 template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
 __global__ void __launch_bounds__(kThreads)
 bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
-  bp_brick<PT, MODE, LANE_Y, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.y, blockIdx.z, smem, false);
+  bp_brick<PT, MODE, LANE_Y, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
 }
 
 template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
@@ -295,7 +297,7 @@ cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cud
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int BX = LANE_Y ? kConsumerWarps : 32, BY = LANE_Y ? 32 : kConsumerWarps;
-  const dim3 grid((P.vol.NX + BX - 1) / BX, (P.vol.NY + BY - 1) / BY, (P.z1 - P.z0 + NZ - 1) / NZ);
+  const dim3 grid((P.vol.NX + BX - 1) / BX, (P.z1 - P.z0 + NZ - 1) / NZ, (P.vol.NY + BY - 1) / BY);
   kern<<<grid, kThreads, smem, st>>>(map, P);
   return cudaGetLastError();
 }
@@ -320,25 +322,47 @@ namespace {
 // cost (most angles first) so the tail is short.  Between items every warp
 // (producer included) meets at a barrier, then the mbarriers are
 // re-initialised for the next brick.
-__global__ void __launch_bounds__(kThreads)
-bp_batch_kernel(const BpBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items, int* err) {
+
+template <int NZ>
+__device__ __forceinline__ void bp_batch_item(const CUtensorMap* map, const BpArgs& P, const int* b,
+                                              unsigned char* smem, bool reinit) {
+  switch (b[4]) {
+    case 0: bp_brick<float, 1, false, false, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+    case 1: bp_brick<float, 1, false, true, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+    case 2: bp_brick<float, 1, true, false, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+    default: bp_brick<float, 1, true, true, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+  }
+}
+
+__global__ void __launch_bounds__(kThreads, 5)
+bp_batch_kernel(const BpBatchDesc* __restrict__ descs, const long long* __restrict__ first, int n_desc,
+                long long n_items, int* err) {
   extern __shared__ __align__(128) unsigned char smem[];
-  constexpr int NZ = kBatchBpNZ;
-  bool first = true;
+  // The item's arguments are staged in shared memory: read from there (like
+  // the constant bank of a single launch) they cost no registers.
+  __shared__ BpArgs sP;
+  __shared__ const CUtensorMap* sMap;
+  __shared__ int sB[5];  // brick x, y, z, depth, lane_y * 2 + bz0
   for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
-    if (!first) __syncthreads();
-    const int2 item = items[it];
-    const BpBatchDesc& D = descs[item.x];
-    const BpArgs P{D.ax, D.vol, D.vol.Zs, D.vol.Zs + D.vol.NZ, D.WX, D.WY, D.align, 1, D.step, D.vol_out,
-                   const_cast<float*>(D.cbp), D.vol_copy, D.copy_kind, err};
-    const int bx = item.y % D.gx, by = (item.y / D.gx) % D.gy, bz = item.y / (D.gx * D.gy);
-    switch (D.lane_y * 2 + D.bz0) {
-      case 0: bp_brick<float, 1, false, false, NZ>(D.map, P, bx, by, bz, smem, !first); break;
-      case 1: bp_brick<float, 1, false, true, NZ>(D.map, P, bx, by, bz, smem, !first); break;
-      case 2: bp_brick<float, 1, true, false, NZ>(D.map, P, bx, by, bz, smem, !first); break;
-      default: bp_brick<float, 1, true, true, NZ>(D.map, P, bx, by, bz, smem, !first); break;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int2 item = work_item(first, n_desc, it);
+      const BpBatchDesc& D = descs[item.x];
+      sP = BpArgs{D.ax, D.vol, D.vol.Zs, D.vol.Zs + D.vol.NZ, D.WX, D.WY, D.align, 1, D.step, D.vol_out,
+                  const_cast<float*>(D.cbp), D.vol_copy, D.copy_kind, err};
+      sMap = D.map;
+      const int gz = (D.vol.NZ + D.nz - 1) / D.nz;  // x fastest, then z, then y (as bp_tma_kernel)
+      sB[0] = item.y % D.gx;
+      sB[2] = (item.y / D.gx) % gz;
+      sB[1] = item.y / (D.gx * gz);
+      sB[3] = D.nz;
+      sB[4] = D.lane_y * 2 + D.bz0;
     }
-    first = false;
+    __syncthreads();
+    const bool reinit = it != blockIdx.x;
+    if (sB[3] == 4) bp_batch_item<4>(sMap, sP, sB, smem, reinit);
+    else if (sB[3] == 16) bp_batch_item<16>(sMap, sP, sB, smem, reinit);
+    else bp_batch_item<8>(sMap, sP, sB, smem, reinit);
   }
 }
 
@@ -354,11 +378,11 @@ int backproject_batch_ctas_per_sm(size_t smem) {
   return n > 0 ? n : 1;
 }
 
-cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const int2* items, long long n_items, size_t smem,
-                                     int grid, int* err, cudaStream_t st) {
+cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const long long* first, int n_desc, long long n_items,
+                                     size_t smem, int grid, int* err, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(bp_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  bp_batch_kernel<<<grid, kThreads, smem, st>>>(descs, items, n_items, err);
+  bp_batch_kernel<<<grid, kThreads, smem, st>>>(descs, first, n_desc, n_items, err);
   return cudaGetLastError();
 }
 
@@ -420,9 +444,6 @@ cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, c
 template cudaError_t launch_backproject_tma<float>(const CUtensorMap&, const BpPlan&, const AxisDev&, const VolDev&,
                                                    int, float, float*, float*, void*, int, int, int, int*,
                                                    cudaStream_t);
-template cudaError_t launch_backproject_tma<__half>(const CUtensorMap&, const BpPlan&, const AxisDev&, const VolDev&,
-                                                    int, float, float*, float*, void*, int, int, int, int*,
-                                                    cudaStream_t);
 
 // ---- host: tensor-map encoding via the driver entry point -------------------
 namespace {

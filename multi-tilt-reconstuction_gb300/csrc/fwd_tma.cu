@@ -361,25 +361,44 @@ namespace {
 // brick): each CTA takes items blockIdx.x, blockIdx.x + gridDim.x, ...; every
 // brick ends with its bulk reduces complete, so the next one reuses the
 // shared-memory windows after a barrier.
+template <typename VT, int NZ>
+__device__ __forceinline__ void fwd_batch_item(const CUtensorMap* map, const FwdArgs& P, const int* b,
+                                               unsigned char* smem) {
+  if (b[4] == 3) fwd_brick<VT, true, true, NZ>(map, P, b[0], b[1], b[2], 0, smem);
+  else fwd_brick<VT, false, true, NZ>(map, P, b[0], b[1], b[2], 0, smem);
+}
+
 template <typename VT>
 __global__ void __launch_bounds__(kThreads)
-fwd_batch_kernel(const FwdBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items) {
+fwd_batch_kernel(const FwdBatchDesc* __restrict__ descs, const long long* __restrict__ first, int n_desc,
+                 long long n_items) {
   extern __shared__ __align__(128) unsigned char smem[];
-  constexpr int NZ = kBatchFwdNZ;
-  bool first = true;
+  // The item's arguments are staged in shared memory (no registers held).
+  __shared__ FwdArgs sP;
+  __shared__ const CUtensorMap* sMap;
+  __shared__ int sB[5];  // brick x, y, z, depth, lane_y * 2 + bz0
   for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
-    if (!first) __syncthreads();
-    const int2 item = items[it];
-    const FwdBatchDesc& D = descs[item.x];
-    const FwdArgs P{D.ax, D.vol, D.vol.Zs, D.vol.Zs + D.vol.NZ, D.WX, D.WY, 1, D.ax.A, D.mass_shift, D.x, nullptr};
-    const int bx = item.y % D.gx, by = (item.y / D.gx) % D.gy, bz = item.y / (D.gx * D.gy);
-    switch (D.lane_y * 2 + D.bz0) {
-      case 0: fwd_brick<VT, false, false, NZ>(D.map, P, bx, by, bz, 0, smem); break;
-      case 1: fwd_brick<VT, false, true, NZ>(D.map, P, bx, by, bz, 0, smem); break;
-      case 2: fwd_brick<VT, true, false, NZ>(D.map, P, bx, by, bz, 0, smem); break;
-      default: fwd_brick<VT, true, true, NZ>(D.map, P, bx, by, bz, 0, smem); break;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const int2 item = work_item(first, n_desc, it);
+      const FwdBatchDesc& D = descs[item.x];
+      sP = FwdArgs{D.ax, D.vol, D.vol.Zs, D.vol.Zs + D.vol.NZ, D.WX, D.WY, 1, D.ax.A, D.mass_shift, D.x, nullptr};
+      sMap = D.map;
+      sB[0] = item.y % D.gx;
+      sB[1] = (item.y / D.gx) % D.gy;
+      sB[2] = item.y / (D.gx * D.gy);
+      sB[3] = D.nz;
+      sB[4] = D.lane_y * 2 + D.bz0;
     }
-    first = false;
+    __syncthreads();
+    switch (sB[4]) {
+      case 0: fwd_brick<VT, false, false, 16>(sMap, sP, sB[0], sB[1], sB[2], 0, smem); break;  // z-dependent y-map
+      case 2: fwd_brick<VT, true, false, 16>(sMap, sP, sB[0], sB[1], sB[2], 0, smem); break;
+      default:
+        if (sB[3] == 8) fwd_batch_item<VT, 8>(sMap, sP, sB, smem);
+        else if (sB[3] == 32) fwd_batch_item<VT, 32>(sMap, sP, sB, smem);
+        else fwd_batch_item<VT, 16>(sMap, sP, sB, smem);
+    }
   }
 }
 
@@ -398,23 +417,23 @@ int forward_batch_ctas_per_sm(size_t smem) {
 }
 
 template <typename VT>
-cudaError_t launch_forward_batch(const FwdBatchDesc* descs, const int2* items, long long n_items, size_t smem,
-                                 int grid, cudaStream_t st) {
+cudaError_t launch_forward_batch(const FwdBatchDesc* descs, const long long* first, int n_desc, long long n_items,
+                                 size_t smem, int grid, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(fwd_batch_kernel<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  fwd_batch_kernel<VT><<<grid, kThreads, smem, st>>>(descs, items, n_items);
+  fwd_batch_kernel<VT><<<grid, kThreads, smem, st>>>(descs, first, n_desc, n_items);
   return cudaGetLastError();
 }
 
 template int forward_batch_ctas_per_sm<float>(size_t);
 template int forward_batch_ctas_per_sm<__nv_bfloat16>(size_t);
 template int forward_batch_ctas_per_sm<__half>(size_t);
-template cudaError_t launch_forward_batch<float>(const FwdBatchDesc*, const int2*, long long, size_t, int,
-                                                 cudaStream_t);
-template cudaError_t launch_forward_batch<__nv_bfloat16>(const FwdBatchDesc*, const int2*, long long, size_t, int,
-                                                         cudaStream_t);
-template cudaError_t launch_forward_batch<__half>(const FwdBatchDesc*, const int2*, long long, size_t, int,
-                                                  cudaStream_t);
+template cudaError_t launch_forward_batch<float>(const FwdBatchDesc*, const long long*, int, long long, size_t,
+                                                  int, cudaStream_t);
+template cudaError_t launch_forward_batch<__nv_bfloat16>(const FwdBatchDesc*, const long long*, int, long long,
+                                                          size_t, int, cudaStream_t);
+template cudaError_t launch_forward_batch<__half>(const FwdBatchDesc*, const long long*, int, long long, size_t,
+                                                   int, cudaStream_t);
 
 FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch,
                      int nz, int lane) {

@@ -54,6 +54,11 @@ __global__ void convert_kernel(const float* __restrict__ src, void* __restrict__
   }
 }
 
+__global__ void widen_kernel(const __half* __restrict__ src, float* __restrict__ dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = __half2float(src[i]);
+}
+
 // One MACE outer step for all K axes at once, replacing the reference's
 // initialZdata + runMaceOnCPU + Reduce/Bcast consensus (FunctionOnGPU.cu:268-313,
 // MultiAxis.cpp:48-67).  On entry x[k] holds v_k = SIRT(z_k), w[k] the state
@@ -119,9 +124,10 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
 // MACE step over many reconstructions: item = (descriptor, chunk of voxels);
 // the arithmetic is mace_kernel's (reference float rounding, FP64 consensus).
 __global__ void __launch_bounds__(kThreads)
-mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items) {
+mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __restrict__ first, int n_desc,
+                  long long n_items) {
   for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
-    const int2 item = items[it];
+    const int2 item = work_item(first, n_desc, it);
     const MaceBatchDesc& D = descs[item.x];
     const long long i0 = (long long)item.y * kBatchChunk;
     const long long i1 = min(D.n, i0 + kBatchChunk);
@@ -156,8 +162,9 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const int2* __restric
 
 }  // namespace
 
-void launch_mace_batch(const MaceBatchDesc* descs, const int2* items, long long n_items, int grid, cudaStream_t st) {
-  mace_batch_kernel<<<grid, kThreads, 0, st>>>(descs, items, n_items);
+void launch_mace_batch(const MaceBatchDesc* descs, const long long* first, int n_desc, long long n_items, int grid,
+                       cudaStream_t st) {
+  mace_batch_kernel<<<grid, kThreads, 0, st>>>(descs, first, n_desc, n_items);
 }
 
 void launch_fill(float* p, long long n, float v, cudaStream_t st) {
@@ -174,6 +181,9 @@ void launch_update_w(const float* v, const float* z, float* w, long long n, floa
 }
 void launch_convert_copy(const float* src, void* dst, int copy_kind, long long n, cudaStream_t st) {
   convert_kernel<<<grid_for(n), kThreads, 0, st>>>(src, dst, copy_kind, n);
+}
+void launch_widen(const __half* src, float* dst, long long n, cudaStream_t st) {
+  widen_kernel<<<grid_for(n), kThreads, 0, st>>>(src, dst, n);
 }
 void launch_mace(int K, float* const* w, float* const* x, float* wavg, long long n, float rho, void* const* x_copy,
                  int copy_kind, double* dchange, cudaStream_t st) {

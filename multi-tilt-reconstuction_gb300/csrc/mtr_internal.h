@@ -114,7 +114,7 @@ struct BpBatchDesc {
   VolDev vol;
   int WX, WY, align;
   int gx, gy;            // brick grid in X and Y
-  int lane_y, bz0;
+  int lane_y, bz0, nz;   // lane axis, z-independent y-map, brick depth (4, 8 or 16)
   float step;
   float* vol_out;        // SIRT iterate (updated in place)
   const float* cbp;      // back-projection weight sums
@@ -127,7 +127,7 @@ struct FwdBatchDesc {
   VolDev vol;
   int WX, WY, mass_shift;
   int gx, gy;
-  int lane_y, bz0;
+  int lane_y, bz0, nz;   // brick depth 8, 16 or 32 (16 when the y-map depends on z)
   const void* x;         // volume read by the splat (float / bf16 / f16)
   const CUtensorMap* map;  // device address of the ray-sum tensor map
 };
@@ -150,20 +150,34 @@ struct MaceBatchDesc {
 };
 constexpr int kBatchChunk = 1 << 16;  // elements per residual / MACE work item
 
-// NZ: brick depth of the batch (8 for the back-projection, 16 for the forward).
-cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const int2* items, long long n_items, size_t smem,
-                                     int grid, int* err, cudaStream_t st);
+// Work list of a persistent kernel: descriptor d owns the items
+// [first[d], first[d+1]) (first[n] = total); descriptors are stored in the
+// order their items should be taken (most costly first).
+#ifdef __CUDACC__
+__device__ __forceinline__ int2 work_item(const long long* __restrict__ first, int n, long long it) {
+  int lo = 0, hi = n - 1;  // the last descriptor with first[d] <= it
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= it) lo = mid;
+    else hi = mid - 1;
+  }
+  return make_int2(lo, (int)(it - first[lo]));
+}
+#endif
+
+// Each descriptor carries the brick depth and lane axis its axis was tuned to.
+cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const long long* first, int n_desc, long long n_items,
+                                     size_t smem, int grid, int* err, cudaStream_t st);
 template <typename VT>
-cudaError_t launch_forward_batch(const FwdBatchDesc* descs, const int2* items, long long n_items, size_t smem,
-                                 int grid, cudaStream_t st);
+cudaError_t launch_forward_batch(const FwdBatchDesc* descs, const long long* first, int n_desc, long long n_items,
+                                 size_t smem, int grid, cudaStream_t st);
 int backproject_batch_ctas_per_sm(size_t smem);
 template <typename VT>
 int forward_batch_ctas_per_sm(size_t smem);
-constexpr int kBatchBpNZ = 8;
-constexpr int kBatchFwdNZ = 16;
-void launch_residual_batch(const ResBatchDesc* descs, const int2* items, long long n_items, int half_b, int grid,
-                           cudaStream_t st);
-void launch_mace_batch(const MaceBatchDesc* descs, const int2* items, long long n_items, int grid, cudaStream_t st);
+void launch_residual_batch(const ResBatchDesc* descs, const long long* first, int n_desc, long long n_items, int half_b,
+                           int grid, cudaStream_t st);
+void launch_mace_batch(const MaceBatchDesc* descs, const long long* first, int n_desc, long long n_items, int grid,
+                       cudaStream_t st);
 
 // ---- elementwise / MACE (mace.cu) ----------------------------------------
 void launch_fill(float* p, long long n, float v, cudaStream_t st);
@@ -174,5 +188,7 @@ void launch_mace(int K, float* const* w, float* const* x, float* wavg, long long
 void launch_initial_z(const float* w, const float* wavg, float* z, long long n, cudaStream_t st);
 void launch_update_w(const float* v, const float* z, float* w, long long n, float step, cudaStream_t st);
 void launch_convert_copy(const float* src, void* dst, int copy_kind, long long n, cudaStream_t st);
+// dst[i] = (float)src[i]: FP16 projections widened for the FP32 WBP kernel.
+void launch_widen(const __half* src, float* dst, long long n, cudaStream_t st);
 
 }  // namespace mtr

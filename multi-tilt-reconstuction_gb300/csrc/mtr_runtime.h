@@ -127,8 +127,8 @@ struct AxisState {
   long long np = 0;       // A*PY*pitch
   std::vector<double> hxc, hyc;  // host copies of the maps (kernel planning)
   BpPlan plan;            // TMA back-projection window plan over r (FP32)
-  BpPlan plan_b;          // ... over b (fp16 when mixed), for the WBP
-  CUtensorMap map_b{}, map_r{};  // tensor maps over b and r
+  BpPlan plan_b;          // WBP plan (FP32 windows, depth 8)
+  CUtensorMap map_b{}, map_r{};  // WBP map over b (FP32) or over r holding b widened (mixed); map over r
   bool tma = false, tma_b = false;
   FwdPlan fplan;          // windowed forward splat plan
   CUtensorMap map_s{}, map_cf{};  // tensor maps over s and cf (valid when ftma)
@@ -137,7 +137,7 @@ struct AxisState {
   DevBuf b;               // projections: float (FP32) or half (mixed)
   DevBuf s;               // forward accumulator, float
   DevBuf cf;              // forward row sums A 1, float
-  DevBuf r;               // residual: float or half
+  DevBuf r;               // residual, float
   DevBuf cbp;             // back-projection weight sums A^T 1 (volume), float
   DevBuf w;               // MACE state w_k (volume), float
   DevBuf x;               // SIRT iterate z_k -> v_k (volume), float
@@ -166,6 +166,26 @@ mtr_status recon_enqueue_init(mtr_recon* r);
 mtr_status recon_enqueue_forward(mtr_recon* r, int k);
 mtr_status recon_enqueue_residual(mtr_recon* r, int k);
 mtr_status recon_enqueue_sirt_bp(mtr_recon* r, int k);
+// MACE step `it` (0-based outer iteration) over all axes of a reconstruction.
+mtr_status recon_enqueue_mace(mtr_recon* r, int it);
+
+// Descriptor tables of the persistent SIRT kernels over a set of
+// reconstructions of one precision (batch.cu).  One SIRT iteration of every
+// axis of every member = one forward, one residual and one back-projection
+// launch over the small axes, plus the own launches of axes large enough to
+// fill the GPU alone and of axes whose windows fit no TMA box.  Device
+// buffers only grow, so rebuilding for a changed set reallocates rarely.
+struct SirtTables {
+  int copy_kind = 0;
+  DevBuf maps, bp_descs, fwd_descs, res_descs, bp_first, fwd_first, res_first;
+  int n_bp_desc = 0, n_fwd_desc = 0, n_res_desc = 0;
+  long long n_bp = 0, n_fwd = 0, n_res = 0;
+  size_t bp_smem = 0, fwd_smem = 0;
+  int bp_grid = 0, fwd_grid = 0, ew_grid = 0;
+  std::vector<std::pair<mtr_recon*, int>> bp_own, fwd_own;  // (reconstruction, axis) with their own launches
+};
+mtr_status build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*>& recs, int precision, SirtTables& t);
+mtr_status enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, int* err);
 
 }  // namespace mtr
 

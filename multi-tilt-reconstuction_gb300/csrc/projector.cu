@@ -235,9 +235,10 @@ residual_kernel(long long n, const BT* __restrict__ b, float* __restrict__ s, co
 // Residual over many axes: item = (descriptor, chunk of kBatchChunk pixels).
 template <bool HALF_B>
 __global__ void __launch_bounds__(256)
-residual_batch_kernel(const ResBatchDesc* __restrict__ descs, const int2* __restrict__ items, long long n_items) {
+residual_batch_kernel(const ResBatchDesc* __restrict__ descs, const long long* __restrict__ first, int n_desc,
+                      long long n_items) {
   for (long long it = blockIdx.x; it < n_items; it += gridDim.x) {
-    const int2 item = items[it];
+    const int2 item = work_item(first, n_desc, it);
     const ResBatchDesc& D = descs[item.x];
     const long long i0 = (long long)item.y * kBatchChunk;
     const long long i1 = min(D.n, i0 + kBatchChunk);
@@ -287,10 +288,10 @@ void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, 
   residual_kernel<BT, RT><<<(unsigned)blocks, 256, 0, st>>>(n, b, s, c, r, norm2);
 }
 
-void launch_residual_batch(const ResBatchDesc* descs, const int2* items, long long n_items, int half_b, int grid,
-                           cudaStream_t st) {
-  if (half_b) residual_batch_kernel<true><<<grid, 256, 0, st>>>(descs, items, n_items);
-  else residual_batch_kernel<false><<<grid, 256, 0, st>>>(descs, items, n_items);
+void launch_residual_batch(const ResBatchDesc* descs, const long long* first, int n_desc, long long n_items, int half_b,
+                           int grid, cudaStream_t st) {
+  if (half_b) residual_batch_kernel<true><<<grid, 256, 0, st>>>(descs, first, n_desc, n_items);
+  else residual_batch_kernel<false><<<grid, 256, 0, st>>>(descs, first, n_desc, n_items);
 }
 
 template void launch_backproject<float>(const AxisDev&, const VolDev&, const float*, int, float, float*, float*,

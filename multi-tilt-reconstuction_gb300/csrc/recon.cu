@@ -142,14 +142,14 @@ mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const void* img_f32_
   // WBP reads the projections (fp16 when mixed), SIRT reads the FP32 residual.
   const bool half_img = mode == 0 && mixed(r->p.precision);
   if ((mode == 0 ? a.tma_b : a.tma) && !img_f32_or_null) {
-    cudaError_t e;
-    if (half_img)
-      e = launch_backproject_tma<__half>(a.map_b, a.plan_b, a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
-                                         a.cbp.as<float>(), a.xcopy.p, ck, z0, z1, r->err.as<int>(), ctx->stream);
-    else
-      e = launch_backproject_tma<float>(mode == 0 ? a.map_b : a.map_r, mode == 0 ? a.plan_b : a.plan, a.dev(), v,
-                                        mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(), a.xcopy.p, ck, z0,
-                                        z1, r->err.as<int>(), ctx->stream);
+    if (half_img) {
+      launch_widen(a.b.as<__half>(), a.r.as<float>(), a.np, ctx->stream);
+      MTR_CK_LAUNCH(ctx, "widen projections");
+    }
+    cudaError_t e = launch_backproject_tma<float>(mode == 0 ? a.map_b : a.map_r, mode == 0 ? a.plan_b : a.plan,
+                                                  a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
+                                                  a.cbp.as<float>(), a.xcopy.p, ck, z0, z1, r->err.as<int>(),
+                                                  ctx->stream);
     g_launches.fetch_add(1);
     if (e != cudaSuccess) return cuda_error(ctx, e, "tma back-projection");
     return MTR_OK;
@@ -218,20 +218,8 @@ namespace {
 mtr_status enqueue_run(mtr_recon* r) {
   mtr_status st = recon_enqueue_init(r);
   if (st != MTR_OK) return st;
-  mtr_context* ctx = r->ctx;
-  const long long nv = r->nv;
-  const int ck = copy_kind_of(r->p.precision);
-  float* wavg = r->wavg.as<float>();
   const int K = r->K, ni = r->p.sirt_inner, no = r->p.iter_times;
   double* norms = r->norms.as<double>();
-  double* dch = r->dchange.as<double>();
-  std::vector<float*> ws(K), xs(K);
-  std::vector<void*> xcs(K);
-  for (int k = 0; k < K; ++k) {
-    ws[k] = r->ax[k].w.as<float>();
-    xs[k] = r->ax[k].x.as<float>();
-    xcs[k] = r->ax[k].xcopy.p;
-  }
   for (int it = 0; it < no; ++it) {
     for (int k = 0; k < K; ++k) {
       AxisState& a = r->ax[k];
@@ -244,17 +232,35 @@ mtr_status enqueue_run(mtr_recon* r) {
         if (s != MTR_OK) return s;
       }
     }
-    {
-      ProfScope ps(ctx, MTR_KERNEL_MACE);
-      launch_mace(K, ws.data(), xs.data(), wavg, nv, r->p.mace_step, xcs.data(), ck, dch ? dch + it : nullptr,
-                  ctx->stream);
-    }
-    MTR_CK_LAUNCH(ctx, "mace");
+    st = recon_enqueue_mace(r, it);
+    if (st != MTR_OK) return st;
   }
   return MTR_OK;
 }
 
 }  // namespace
+
+// MACE step `it` of a reconstruction (one fused launch over its K axes).
+mtr_status mtr::recon_enqueue_mace(mtr_recon* r, int it) {
+  mtr_context* ctx = r->ctx;
+  const int K = r->K;
+  float* ws[MTR_MAX_AXES];
+  float* xs[MTR_MAX_AXES];
+  void* xcs[MTR_MAX_AXES];
+  for (int k = 0; k < K; ++k) {
+    ws[k] = r->ax[k].w.as<float>();
+    xs[k] = r->ax[k].x.as<float>();
+    xcs[k] = r->ax[k].xcopy.p;
+  }
+  double* dch = r->dchange.as<double>();
+  {
+    ProfScope ps(ctx, MTR_KERNEL_MACE);
+    launch_mace(K, ws, xs, r->wavg.as<float>(), r->nv, r->p.mace_step, xcs, copy_kind_of(r->p.precision),
+                dch && it < r->p.iter_times ? dch + it : nullptr, ctx->stream);
+  }
+  MTR_CK_LAUNCH(ctx, "mace");
+  return MTR_OK;
+}
 
 extern "C" {
 
@@ -331,9 +337,11 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     if (s != MTR_OK) return s;
     // TMA kernels where the window geometry fits (else the plain kernels run).
     if (!tma_disabled()) {
-      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, mx, 8);  // WBP over b (fp16 when mixed)
-      a.tma_b = a.plan_b.ok &&
-                encode_tensor_map_3d(&a.map_b, a.b.p, mx, a.PX, a.pitch, a.PY, a.A, a.plan_b.WX, a.plan_b.WY);
+      // WBP over b; with FP16 projections over their FP32 widening in r (r is
+      // free until the first residual), so the WBP gathers FP32 like SIRT.
+      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, false, 8);
+      a.tma_b = a.plan_b.ok && encode_tensor_map_3d(&a.map_b, mx ? a.r.p : a.b.p, false, a.PX, a.pitch, a.PY, a.A,
+                                                    a.plan_b.WX, a.plan_b.WY);
       // SIRT back-projection over the FP32 residual and the forward splat: tuned depths
       tune_axis(ctx, a, r->vol, params->precision, a.w.as<float>(), a.cbp.as<float>(), r->err.as<int>());
     }

@@ -99,22 +99,43 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
   return buf;
 }
 
-float time_launches(cudaStream_t st, const std::function<cudaError_t()>& launch, bool* ok) {
+// Times every candidate launch and returns the index of the fastest (-1 if
+// none ran).  Each candidate is launched once untimed, then the candidates
+// are timed round-robin for kRounds rounds and each keeps its minimum, so a
+// clock ramp during tuning does not favour the candidates timed last.
+constexpr int kRounds = 3;
+int fastest(cudaStream_t st, const std::vector<std::function<cudaError_t()>>& cands) {
+  const size_t n = cands.size();
+  std::vector<float> best(n, 1e30f);
+  std::vector<bool> ok(n, false);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
-  *ok = false;
-  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) return 0.f;
-  float ms = 0.f;
-  if (launch() == cudaSuccess) {  // warm-up (module load, attribute set-up)
-    cudaEventRecord(e0, st);
-    const cudaError_t e = launch();
-    cudaEventRecord(e1, st);
-    if (e == cudaSuccess && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess)
-      *ok = true;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    cudaGetLastError();
+    return -1;
   }
+  for (size_t i = 0; i < n; ++i) ok[i] = cands[i]() == cudaSuccess;  // warm-up: module load, attributes
   cudaGetLastError();
+  for (int r = 0; r < kRounds; ++r)
+    for (size_t i = 0; i < n; ++i) {
+      if (!ok[i]) continue;
+      float ms = 0.f;
+      cudaEventRecord(e0, st);
+      const cudaError_t e = cands[i]();
+      cudaEventRecord(e1, st);
+      if (e != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        ok[i] = false;
+        cudaGetLastError();
+        continue;
+      }
+      best[i] = std::min(best[i], ms);
+    }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  return ms;
+  int arg = -1;
+  for (size_t i = 0; i < n; ++i)
+    if (ok[i] && (arg < 0 || best[i] < best[arg])) arg = (int)i;
+  return arg;
 }
 
 }  // namespace
@@ -152,45 +173,65 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
   }
   const int z0 = v.Zs, z1 = v.Zs + v.NZ;
   if (!known && autotune_enabled()) {
-    float best = 1e30f;
+    // back-projection candidates: depth x lane axis
+    std::vector<std::function<cudaError_t()>> cands;
+    std::vector<std::pair<int, int>> what;
+    std::vector<BpPlan> bps;
+    std::vector<CUtensorMap> bmaps;
+    bps.reserve(6);
+    bmaps.reserve(6);
     for (int lane = 0; lane < 2; ++lane)
       for (int nz : kBpDepths) {
         BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, false, nz, lane);
         CUtensorMap m;
         if (!p.ok || !encode_tensor_map_3d(&m, a.r.p, false, a.PX, a.pitch, a.PY, a.A, p.WX, p.WY)) continue;
-        bool ok = false;
-        const float ms = time_launches(ctx->stream, [&] {
-          return launch_backproject_tma<float>(m, p, a.dev(), v, 1, 0.5f, scratch_vol, scratch_cbp, a.xcopy.p,
+        bps.push_back(p);
+        bmaps.push_back(m);
+        const BpPlan* pp = &bps.back();
+        const CUtensorMap* mp = &bmaps.back();
+        cands.push_back([=, &a, &v] {
+          return launch_backproject_tma<float>(*mp, *pp, a.dev(), v, 1, 0.5f, scratch_vol, scratch_cbp, a.xcopy.p,
                                                copy_kind, z0, z1, err, ctx->stream);
-        }, &ok);
-        if (ok && ms < best) {
-          best = ms;
-          ch.bp_nz = nz;
-          ch.bp_lane = lane;
-        }
+        });
+        what.push_back({nz, lane});
       }
-    best = 1e30f;
+    int k = fastest(ctx->stream, cands);
+    if (k >= 0) {
+      ch.bp_nz = what[k].first;
+      ch.bp_lane = what[k].second;
+    }
+    // forward candidates
+    cands.clear();
+    what.clear();
+    std::vector<FwdPlan> fps;
+    std::vector<CUtensorMap> fmaps;
+    fps.reserve(6);
+    fmaps.reserve(6);
     for (int lane = 0; lane < 2; ++lane)
       for (int nz : kFwdDepths) {
         FwdPlan p = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, nz, lane);
         CUtensorMap m;
         if (!p.ok || p.nz != nz || !encode_tensor_map_3d(&m, a.s.p, false, a.pitch, a.pitch, a.PY, a.A, p.WX, p.WY))
           continue;
-        bool ok = false;
-        const float ms = time_launches(ctx->stream, [&] {
+        fps.push_back(p);
+        fmaps.push_back(m);
+        const FwdPlan* pp = &fps.back();
+        const CUtensorMap* mp = &fmaps.back();
+        cands.push_back([=, &a, &v] {
           if (copy_kind == 1)
-            return launch_forward_tma<__nv_bfloat16>(m, p, a.dev(), v, a.xcopy.as<__nv_bfloat16>(), z0, z1, err,
+            return launch_forward_tma<__nv_bfloat16>(*mp, *pp, a.dev(), v, a.xcopy.as<__nv_bfloat16>(), z0, z1, err,
                                                      ctx->stream);
           if (copy_kind == 2)
-            return launch_forward_tma<__half>(m, p, a.dev(), v, a.xcopy.as<__half>(), z0, z1, err, ctx->stream);
-          return launch_forward_tma<float>(m, p, a.dev(), v, a.x.as<float>(), z0, z1, err, ctx->stream);
-        }, &ok);
-        if (ok && ms < best) {
-          best = ms;
-          ch.fwd_nz = nz;
-          ch.fwd_lane = lane;
-        }
+            return launch_forward_tma<__half>(*mp, *pp, a.dev(), v, a.xcopy.as<__half>(), z0, z1, err, ctx->stream);
+          return launch_forward_tma<float>(*mp, *pp, a.dev(), v, a.x.as<float>(), z0, z1, err, ctx->stream);
+        });
+        what.push_back({nz, lane});
       }
+    k = fastest(ctx->stream, cands);
+    if (k >= 0) {
+      ch.fwd_nz = what[k].first;
+      ch.fwd_lane = what[k].second;
+    }
     std::lock_guard<std::mutex> lock(g_mu);
     g_cache[key] = ch;
     save_file();

@@ -65,6 +65,17 @@ class InstanceC(C.Structure):
     _fields_ = [("n_axes", C.c_int), ("axes", C.POINTER(AxisC)), ("vol", VolumeSize)]
 
 
+class RequestC(C.Structure):
+    _fields_ = [("n_axes", C.c_int), ("axes", C.POINTER(AxisC)), ("vol", VolumeSize), ("iter_times", C.c_int),
+                ("sirt_inner", C.c_int), ("sirt_step", C.c_float), ("mace_step", C.c_float),
+                ("out", C.POINTER(C.c_float))]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_longlong) for n in ("submitted", "completed", "queued", "active", "bytes_in_use",
+                                             "peak_bytes", "budget_bytes", "steps", "voxel_updates")]
+
+
 class Params(C.Structure):
     _fields_ = [("iter_times", C.c_int), ("sirt_inner", C.c_int), ("sirt_step", C.c_float),
                 ("mace_step", C.c_float), ("precision", C.c_int), ("flags", C.c_int)]
@@ -134,6 +145,11 @@ _SIGNATURES = {
     "mtr_batch_download": (C.c_int, [_P, C.c_int, _P, C.c_int]),
     "mtr_batch_info": (C.c_int, [_P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "mtr_batch_destroy": (C.c_int, [_P]),
+    "mtr_server_create": (C.c_int, [_P, C.c_longlong, C.c_int, C.POINTER(_P)]),
+    "mtr_server_submit": (C.c_int, [_P, C.POINTER(RequestC), C.POINTER(C.c_longlong)]),
+    "mtr_server_step": (C.c_int, [_P, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
+    "mtr_server_stats_get": (C.c_int, [_P, C.POINTER(ServerStats)]),
+    "mtr_server_destroy": (C.c_int, [_P]),
     "mtr_mrc_read_header": (C.c_int, [C.c_char_p, C.POINTER(MrcHeader)]),
     "mtr_mrc_read_stack": (C.c_int, [C.c_char_p, _P, C.c_longlong]),
     "mtr_txbr_read": (C.c_int, [C.c_char_p, _P, _P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -396,11 +412,70 @@ class Batch:
         items = (C.c_longlong * 5)()
         self.ctx.check(self.ctx.lib.mtr_batch_info(self.h, C.byref(vu), C.byref(by), items), "mtr_batch_info")
         return {"voxel_updates": vu.value, "bytes": by.value,
-                "items": dict(zip(["forward", "residual", "backproject", "mace", "fallback_axes"], list(items)))}
+                "items": dict(zip(["forward", "residual", "backproject", "mace", "own_launch_axes"], list(items)))}
 
     def close(self) -> None:
         if self.h:
             self.ctx.lib.mtr_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching server (mtr_server_*): requests are admitted by
+    device footprint under `budget_bytes` and advance one SIRT iteration per
+    step, all admitted requests in one persistent launch per phase."""
+
+    def __init__(self, ctx: Context, budget_bytes: int, precision: int = PREC_FP32):
+        self.ctx = ctx
+        h = _P()
+        ctx.check(ctx.lib.mtr_server_create(ctx.h, int(budget_bytes), precision, C.byref(h)), "mtr_server_create")
+        self.h = h
+        self._keep = {}  # id -> (axis structs, host arrays, output array)
+        self._ids = (C.c_longlong * 4096)()
+
+    def submit(self, axes: Sequence["AxisData"], vol: VolumeSize, iter_times: int, sirt_inner: int = 10,
+               sirt_step: float = 0.5, mace_step: float = 0.7) -> int:
+        if not all(isinstance(a.data, np.ndarray) for a in axes):
+            raise TypeError("server requests take host (numpy) projections")
+        out = np.empty(vol.shape, np.float32)
+        ax = (AxisC * len(axes))(*[a.c_struct() for a in axes])
+        req = RequestC(len(axes), ax, vol, iter_times, sirt_inner, sirt_step, mace_step,
+                       out.ctypes.data_as(C.POINTER(C.c_float)))
+        rid = C.c_longlong()
+        self.ctx.check(self.ctx.lib.mtr_server_submit(self.h, C.byref(req), C.byref(rid)), "mtr_server_submit")
+        self._keep[rid.value] = (ax, list(axes), out)
+        return rid.value
+
+    def step(self) -> list:
+        """One scheduling step; returns [(id, volume)] of the requests retired."""
+        n = C.c_int()
+        self.ctx.check(self.ctx.lib.mtr_server_step(self.h, len(self._ids), self._ids, C.byref(n)), "mtr_server_step")
+        return [(i, self._keep.pop(i)[2]) for i in self._ids[:n.value]]
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self.ctx.check(self.ctx.lib.mtr_server_stats_get(self.h, C.byref(st)), "mtr_server_stats_get")
+        return {n: getattr(st, n) for n, _ in ServerStats._fields_}
+
+    def drain(self, max_steps: int = 1 << 30) -> dict:
+        done = {}
+        for _ in range(max_steps):
+            for i, v in self.step():
+                done[i] = v
+            st = self.stats()
+            if st["queued"] == 0 and st["active"] == 0:
+                break
+        return done
+
+    def close(self) -> None:
+        if self.h:
+            self.ctx.lib.mtr_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

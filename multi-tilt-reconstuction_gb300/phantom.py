@@ -177,37 +177,47 @@ def line_integrals_torch(ell: Ellipsoids, x_coef: np.ndarray, y_coef: np.ndarray
                          device="cuda", ell_chunk: int = 32) -> "object":
     """Same analytic line integrals as line_integrals(), evaluated with torch
     in FP64 on a CUDA device for the large benchmark sizes; returns a float32
-    CUDA tensor [A, py, px]."""
+    CUDA tensor [A, py, px].
+
+    Along the ray through detector pixel (u, v) the offset from an ellipsoid's
+    centre is r = c + u e1 + v e2 + t d, so beta = (Q d).r is linear and
+    gamma = r^T Q r - 1 quadratic in (u, v): their coefficients are formed per
+    ellipsoid on the host and only the polynomials are evaluated per pixel."""
     import torch
 
     A = len(x_coef) // 4
+    f64 = dict(dtype=torch.float64, device=device)
     out = torch.empty((A, py, px), dtype=torch.float32, device=device)
-    Q = torch.as_tensor(ell.Q, dtype=torch.float64, device=device)            # [n,3,3]
-    m = torch.as_tensor(ell.centre, dtype=torch.float64, device=device)       # [n,3]
-    rho = torch.as_tensor(ell.density, dtype=torch.float64, device=device)    # [n]
-    vv, uu = torch.meshgrid(torch.arange(py, dtype=torch.float64, device=device),
-                            torch.arange(px, dtype=torch.float64, device=device), indexing="ij")
+    u = torch.arange(px, **f64)[None, None, :]
+    v = torch.arange(py, **f64)[None, :, None]
+    Q, m, rho = np.asarray(ell.Q, np.float64), np.asarray(ell.centre, np.float64), np.asarray(ell.density, np.float64)
     for k in range(A):
         xc, yc = x_coef[4 * k:4 * k + 4], y_coef[4 * k:4 * k + 4]
         eu, ea = np.asarray(xc[1:]), np.asarray(yc[1:])
         d = np.cross(eu, ea)
         d /= np.linalg.norm(d)
-        Minv = torch.as_tensor(np.linalg.inv(np.stack([eu, ea, d])), dtype=torch.float64, device=device)
-        dd = torch.as_tensor(d, dtype=torch.float64, device=device)
-        p0 = (Minv[:, 0:1, None] * (uu + 1 - xc[0])[None] + Minv[:, 1:2, None] * (vv + 1 - yc[0])[None])  # [3,py,px]
-        p0 = p0.reshape(3, -1)
-        acc = torch.zeros(p0.shape[1], dtype=torch.float64, device=device)
-        Qd = torch.einsum("nij,j->ni", Q, dd)                                   # [n,3]
-        alpha = Qd @ dd                                                          # [n]
-        for s in range(0, len(ell.density), ell_chunk):
-            e = slice(s, s + ell_chunk)
-            r = p0[None] - m[e, :, None]                                         # [c,3,P]
-            beta = torch.einsum("ni,nip->np", Qd[e], r)
-            gamma = torch.einsum("nip,nij,njp->np", r, Q[e], r) - 1.0
-            disc = beta * beta - alpha[e, None] * gamma
-            chord = 2.0 * torch.sqrt(torch.clamp(disc, min=0.0)) / alpha[e, None]
-            acc += (rho[e, None] * chord).sum(0)
-        out[k] = acc.reshape(py, px).to(torch.float32)
+        Minv = np.linalg.inv(np.stack([eu, ea, d]))
+        e1, e2 = Minv[:, 0], Minv[:, 1]
+        c = e1 * (1.0 - xc[0]) + e2 * (1.0 - yc[0]) - m                       # [n,3]
+        Qd = Q @ d                                                               # [n,3]
+        Qc, Qe1, Qe2 = np.einsum("nij,nj->ni", Q, c), Q @ e1, Q @ e2
+        coef = np.stack([
+            Qd @ d,                                                              # alpha
+            np.einsum("ni,ni->n", Qd, c), Qd @ e1, Qd @ e2,                      # beta: 1, u, v
+            np.einsum("ni,ni->n", c, Qc) - 1.0, 2 * np.einsum("ni,ni->n", Qc, np.broadcast_to(e1, c.shape)),
+            2 * np.einsum("ni,ni->n", Qc, np.broadcast_to(e2, c.shape)),         # gamma: 1, u, v
+            Qe1 @ e1, 2 * (Qe1 @ e2), Qe2 @ e2,                                  # gamma: uu, uv, vv
+            rho], axis=1)
+        C = torch.as_tensor(coef, **f64)[:, :, None, None]                       # [n,11,1,1]
+        acc = torch.zeros((py, px), **f64)
+        for s in range(0, len(rho), ell_chunk):
+            K = C[s:s + ell_chunk]
+            al, b0, bu, bv, g0, gu, gv, guu, guv, gvv, dens = K.unbind(1)
+            beta = b0 + bu * u + bv * v
+            gamma = g0 + (gu + guu * u + guv * v) * u + (gv + gvv * v) * v
+            disc = beta * beta - al * gamma
+            acc += (dens * 2.0 * torch.sqrt(torch.clamp(disc, min=0.0)) / al).sum(0)
+        out[k] = acc.to(torch.float32)
     return out
 
 

@@ -11,7 +11,7 @@ from conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
-NAMES = ["mid", "mid_oblique", "two_axis", "four_axis", "single"]  # the last three run on fallback kernels
+NAMES = ["mid", "mid_oblique", "two_axis", "four_axis", "single"]
 
 
 @pytest.mark.parametrize("prec", [mtr.PREC_FP32, mtr.PREC_MIXED_BF16])
