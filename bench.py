@@ -54,8 +54,8 @@ CONFIGS = {
 # Per-launch DRAM traffic and instruction count of the dominant kernel, from
 # the ncu captures summarised in profiles/ (one launch of axis 0).
 NCU_PROFILES = {
-    ("c2", "backproject"): {"traffic": 330_938_368 + 157_545_984, "warp_inst_per_voxel_angle": 1_426_398_948 /
-                            (512 * 512 * 128 * 61), "sms": 152,
+    ("c2", "backproject"): {"traffic": 330_938_368 + 157_545_984, "warp_inst": 1_426_398_948,
+                            "duration_ms": 1.371552, "sm_ghz": 2.07, "sms": 152,
                             "source": "profiles/bp_tma_kernel_3axis_512x512x128.md"},
 }
 
@@ -272,6 +272,10 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
 
     out_mixed = rec.download()
     out_fp32 = ref32.download()
+    # free both device-resident runs before the end-to-end calls allocate their own
+    rec.close()
+    if ref32 is not rec:
+        ref32.close()
 
     # end to end through the public host-buffer API: H2D of the projections from
     # pinned memory, device allocation, geometry sums, the run, D2H of the volume
@@ -282,6 +286,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
         pinned.copy_(a.data)
         host_axes.append(mtr.AxisData(a.x_coef, a.y_coef, pinned.numpy()))
         h2d += pinned.numel() * 4 + a.x_coef.nbytes + a.y_coef.nbytes
+    del axes, a
+    torch.cuda.empty_cache()
     out_pinned = torch.empty(vol.shape, dtype=torch.float32, pin_memory=True).numpy()
     p_e2e = mk(prec)
     arr_ms = []
@@ -301,9 +307,6 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     # error of both paths against the all-FP64 GPU reconstruction of the same inputs
     err64 = None
     if args.fp64 and args.config != "c3":
-        rec.close()
-        if ref32 is not rec:
-            ref32.close()
         t = time.time()
         out64 = ctx.reconstruct_fp64(host_axes, vol, mk(mtr.PREC_FP32))
         n64 = max(float(np.linalg.norm(out64)), 1e-300)
@@ -523,28 +526,38 @@ def run_serve_bench(args) -> dict:
             "gpu_launches": None, "e2e": None}
 
 
+def cpu_slab(vol, n_angles: int) -> int:
+    """Z planes of the CPU sample: the whole volume up to ~2 G voxel-angle
+    evaluations per SIRT iteration (a few seconds on the host cores)."""
+    return int(max(1, min(vol.Z, round(2e9 / (vol.X * vol.Y * n_angles)))))
+
+
 def cpu_baseline(cfg: dict, vol, axes_host, budget_s: float = 20.0) -> dict:
     """Reference-faithful CPU oracle on the host cores: SIRT iterations of axis 0
-    on the full volume (each one = V voxel-updates)."""
+    over a Z-slab (the whole volume up to ~2 G voxel-angle evaluations per
+    iteration; each iteration = slab-voxels voxel-updates)."""
     import oracle
 
     n = os.cpu_count() or 1
     oracle.set_threads(n)
     a = axes_host[0]
-    x0 = np.zeros(vol.shape, np.float64)
+    dz = cpu_slab(vol, a.data.shape[0])
+    z0, z1 = vol.Zstart, vol.Zstart + dz
+    x0 = np.zeros((dz, vol.Y, vol.X), np.float64)
     t = time.perf_counter()
     it = 0
     while True:
-        oracle.sirt(oracle.REF_FAITHFUL, a, vol, x0, 1, cfg["sirt_step"])
+        oracle.sirt(oracle.REF_FAITHFUL, a, vol, x0, 1, cfg["sirt_step"], z0, z1)
         it += 1
         el = time.perf_counter() - t
         if el > budget_s / 2 or it >= 3:
             break
-    V = vol.X * vol.Y * vol.Z
+    V = vol.X * vol.Y * dz
+    where = (f"the full {vol.X}x{vol.Y}x{vol.Z} volume" if dz == vol.Z else
+             f"a {dz}-plane Z-slab of the {vol.X}x{vol.Y}x{vol.Z} volume")
     return {"value": V * it / el, "unit": UNIT, "cores": n, "kind": "port",
             "sample": f"{it} reference-faithful SIRT iteration(s) (forward splat + residual + back-projection) of "
-                      f"axis 0 over the full {vol.X}x{vol.Y}x{vol.Z} volume, OpenMP over {n} host threads, "
-                      f"{el:.1f} s"}
+                      f"axis 0 over {where}, OpenMP over {n} host threads, {el:.1f} s"}
 
 
 def run_reference(args) -> dict:
@@ -562,14 +575,17 @@ def run_reference(args) -> dict:
     host = mtr.AxisData(a.x_coef, a.y_coef, a.data.cpu().numpy() if hasattr(a.data, "cpu") else a.data)
     n = os.cpu_count() or 1
     oracle.set_threads(n)
-    x0 = np.zeros(vol.shape, np.float64)
+    dz = cpu_slab(vol, host.data.shape[0])
+    z0, z1 = vol.Zstart, vol.Zstart + dz
+    x0 = np.zeros((dz, vol.Y, vol.X), np.float64)
     for _ in range(args.warmup):
-        oracle.sirt(oracle.REF_FAITHFUL, host, vol, x0, 1, cfg["sirt_step"])
+        oracle.sirt(oracle.REF_FAITHFUL, host, vol, x0, 1, cfg["sirt_step"], z0, z1)
     t = time.perf_counter()
     for _ in range(args.steps):
-        oracle.sirt(oracle.REF_FAITHFUL, host, vol, x0, 1, cfg["sirt_step"])
+        oracle.sirt(oracle.REF_FAITHFUL, host, vol, x0, 1, cfg["sirt_step"], z0, z1)
     el = time.perf_counter() - t
-    V = vol.X * vol.Y * vol.Z
+    V = vol.X * vol.Y * dz
+    where = "the full volume" if dz == vol.Z else f"a {dz}-plane Z-slab"
     value = V * args.steps / el
     return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps * 1e3,
@@ -577,7 +593,7 @@ def run_reference(args) -> dict:
             "config": {"workload": cfg["workload"], "step": "one SIRT iteration of axis 0 (bounded sample)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": n, "kind": "port",
                              "sample": f"reference-faithful CPU restatement (the reference's path is CUDA+MPI only), "
-                                       f"one SIRT iteration of axis 0 over the full volume per step, {n} threads"},
+                                       f"one SIRT iteration of axis 0 over {where} per step, {n} threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -642,15 +658,14 @@ def main() -> int:
                 "avg_launch_ms": per_launch_ms, "launches": n_l,
                 "kernel_share": {k: prof[k][1] / max(sum(x[1] for x in prof.values()), 1e-9) for k in prof}}
         if ncu:
-            # the roof that binds: instruction issue (ncu instruction count per
-            # voxel-angle x live launch rate, against 4 issue slots per SM per clock)
-            va = cfg_voxel_angles(cfg)
-            issue_peak = ncu["sms"] * 4 * (r["clk"]["sm_mhz"] or 2070.0) * 1e6
-            inst_rate = ncu["warp_inst_per_voxel_angle"] * va / (per_launch_ms * 1e-3)
+            # the roof that binds is instruction issue; figures of the captured
+            # launch (axis 0) against 4 issue slots per SM per clock
+            issue_peak = ncu["sms"] * 4 * ncu["sm_ghz"] * 1e9
+            inst_rate = ncu["warp_inst"] / (ncu["duration_ms"] * 1e-3)
             roof["binding"] = {"resource": "instruction issue", "achieved": inst_rate, "peak": issue_peak,
                                "unit": "warp-instructions/s", "frac": inst_rate / issue_peak,
-                               "warp_inst_per_voxel_angle": ncu["warp_inst_per_voxel_angle"],
-                               "source": ncu["source"]}
+                               "warp_inst_per_voxel_angle": ncu["warp_inst"] / cfg_voxel_angles(cfg),
+                               "launch": "axis 0 (ncu)", "source": ncu["source"]}
         vu = r["vu"] * world
         value = replica_value(r["vu"], world, r["ms"])
         line = {

@@ -345,6 +345,34 @@ mtr_status mtr_mrc_read_stack(const char* path, float* out, long long n);
  * the x->, y->, z-> bound lines and sets vol->X/Y/Z = end - start. */
 mtr_status mtr_txbr_read(const char* path, double* x_coef, double* y_coef, int cap, int* n_x, int* n_y,
                          mtr_volume_size* vol);
+/* ---- Geometry front end: tilt angles and 2-D alignments -> linear maps ----
+ * No counterpart in the reference, which only reads precomputed linear maps
+ * (readCoef, MrcFileIOBaseFunction.cpp:72-134).  These build the same
+ * per-view maps x = c0 + c1 X + c2 Y + c3 Z (1-based detector pixel
+ * coordinates of voxel (X, Y, Z), the TXBR coefficient order) from a
+ * parallel-beam tilt series.
+ *
+ * Aligned view k of tilt angle t about an axis at in-plane angle phi:
+ *   u_al - cu = cos(t) (cos(phi) (X-cx) + sin(phi) (Y-cy)) + sin(t) (Z-cz)
+ *   v_al - cv = -sin(phi) (X-cx) + cos(phi) (Y-cy)
+ * with detector centre (cu, cv) = ((det_x+1)/2, (det_y+1)/2) and volume
+ * centre c = ((Xstart+Xend-1)/2, ...).  An alignment transform (IMOD .xf
+ * convention: rows "a11 a12 a21 a22 dx dy", applied about the image centre)
+ * maps raw view coordinates to aligned ones,
+ *   al - C = A (raw - C) + (dx, dy),
+ * so the maps returned address the RAW view: raw = C + A^-1 (al - C - d).
+ * xf == NULL means identity for every view.  Fails with
+ * MTR_ERR_INVALID_ARGUMENT for a singular A or a non-finite input. */
+typedef struct mtr_xf {
+  double a11, a12, a21, a22, dx, dy;
+} mtr_xf;
+mtr_status mtr_geometry_from_tilts(int n_views, const double* tilt_deg, const mtr_xf* xf, double phi_deg, int det_x,
+                                   int det_y, mtr_volume_size vol, double* x_coef, double* y_coef);
+/* One angle per line (IMOD .tlt); reads up to cap values into *n. */
+mtr_status mtr_tlt_read(const char* path, double* tilt_deg, int cap, int* n);
+/* Six numbers per line "a11 a12 a21 a22 dx dy" (IMOD .xf); up to cap views. */
+mtr_status mtr_xf_read(const char* path, mtr_xf* xf, int cap, int* n);
+
 /* Initialise a volume frame to the reference's empty bounds
  * (Xstart=999999, Xend=-999999, ..., MrcFileIO.h:22-28). */
 void mtr_volume_size_empty(mtr_volume_size* vol);

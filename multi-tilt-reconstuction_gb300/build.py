@@ -29,7 +29,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", "-I"
 
 CU_SOURCES = ["projector.cu", "bp_tma.cu", "fwd_tma.cu", "mace.cu", "api.cu", "recon.cu", "entry.cu", "ref64.cu",
               "noalloc.cu", "tune.cu", "batch.cu", "serve.cu"]
-CXX_SOURCES = ["mrc_io.cpp", "options.cpp"]
+CXX_SOURCES = ["mrc_io.cpp", "options.cpp", "geometry.cpp"]
 
 
 def nvcc() -> str:

@@ -63,6 +63,40 @@ __device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b
 
 __device__ __forceinline__ int magic_int(float integral) { return __float_as_int(__fadd_rn(integral, kMagic)); }
 
+// Gather of one voxel column (fixed X, Y; y-map without a Z term) from
+// detector rows `row0` and `row0 + WX`, adding into s[0..NZ).  x advances by
+// |a3| < 1 per voxel, so the fraction is stepped by one add and the tap
+// pointer by a predicated increment instead of a floor per voxel.  ASC walks
+// z upwards (a3 >= 0), else downwards, so that x never decreases.  Rounding
+// of the stepped fraction stays below 4e-6 px over 32 voxels; the caller
+// leaves one pixel of window slack for it.
+template <bool ASC, int NZ, typename PT>
+__device__ __forceinline__ void bp_column(float (&s)[NZ], const PT* row0, int WX, float xr, float a3, int lxm,
+                                          float wy0, float wy1) {
+  constexpr int zf = ASC ? 0 : NZ - 1;
+  const float x = fmaf(a3, (float)zf, xr);
+  const float flx = floorf(x);
+  float fx = x - flx;
+  const float step = fabsf(a3);
+  const PT* p = row0 + (magic_int(flx) + lxm);
+#pragma unroll
+  for (int i = 0; i < NZ; ++i) {
+    const int z = ASC ? i : NZ - 1 - i;
+    if (i > 0) {
+      fx += step;
+      const bool adv = fx >= 1.f;
+      fx = adv ? fx - 1.f : fx;
+      p += adv ? 1 : 0;
+    }
+    const float p00 = to_f(p[0]), p10 = to_f(p[1]);
+    const float p01 = to_f(p[WX]), p11 = to_f(p[WX + 1]);
+    const float r0 = fmaf(fx, p10 - p00, p00);
+    const float r1 = fmaf(fx, p11 - p01, p01);
+    s[z] = fmaf(wy0, r0, s[z]);
+    s[z] = fmaf(wy1, r1, s[z]);
+  }
+}
+
 // One brick (bx, by, bz) of one axis.  LANE_Y: consecutive lanes walk Y (used
 // when the detector x follows Y).  `smem` is the CTA's dynamic shared memory;
 // `reinit` re-initialises the mbarriers of a CTA that already ran a brick.
@@ -171,34 +205,24 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
     const WinConst k = kc[a];
     const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
     const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
-    if (active && BZ0 && MODE == 1) {
+    bool done = !active;
+    if (active && BZ0 && MODE == 1 && fabsf(k.a3) < 0.999f) {
       // x is affine in z: the column's end voxels bound every tap index, so
-      // the window bound is checked once per column instead of per voxel.
+      // the window bound is checked once per column instead of per voxel; the
+      // stepped tap may run one pixel past the exact last one.
       const float fly = floorf(yr);
       const float fy = yr - fly;
       const int rowi = magic_int(fly) + k.lym;
       const int ixa = magic_int(floorf(xr)) + k.lxm;
       const int ixb = magic_int(floorf(fmaf(k.a3, (float)(NZ - 1), xr))) + k.lxm;
-      if ((unsigned)rowi >= lim_y || (unsigned)ixa >= lim_x || (unsigned)ixb >= lim_x) {
-        bad = true;
-      } else {
+      if ((unsigned)rowi < lim_y && (unsigned)min(ixa, ixb) < lim_x && (unsigned)(max(ixa, ixb) + 1) < lim_x) {
         const PT* row0 = w + rowi * WX;
-        const float wy0 = 1.f - fy, wy1 = fy;
-#pragma unroll
-        for (int z = 0; z < NZ; ++z) {
-          const float x = fmaf(k.a3, (float)z, xr);
-          const float flx = floorf(x);
-          const float fx = x - flx;
-          const PT* p = row0 + (magic_int(flx) + k.lxm);
-          const float p00 = to_f(p[0]), p10 = to_f(p[1]);
-          const float p01 = to_f(p[WX]), p11 = to_f(p[WX + 1]);
-          const float r0 = fmaf(fx, p10 - p00, p00);
-          const float r1 = fmaf(fx, p11 - p01, p01);
-          s[z] = fmaf(wy0, r0, s[z]);
-          s[z] = fmaf(wy1, r1, s[z]);
-        }
+        if (k.a3 >= 0.f) bp_column<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+        else bp_column<false, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+        done = true;
       }
-    } else if (active) {
+    }
+    if (!done) {
       // y part (per column when the map has no Z term)
       float fy = 0.f, wy0 = 0.f, wy1 = 0.f, cy = 0.f;
       int rowi = 0;

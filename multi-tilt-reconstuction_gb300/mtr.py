@@ -71,6 +71,10 @@ class RequestC(C.Structure):
                 ("out", C.POINTER(C.c_float))]
 
 
+class XF(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("a11", "a12", "a21", "a22", "dx", "dy")]
+
+
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_longlong) for n in ("submitted", "completed", "queued", "active", "bytes_in_use",
                                              "peak_bytes", "budget_bytes", "steps", "voxel_updates")]
@@ -145,6 +149,10 @@ _SIGNATURES = {
     "mtr_batch_download": (C.c_int, [_P, C.c_int, _P, C.c_int]),
     "mtr_batch_info": (C.c_int, [_P, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]),
     "mtr_batch_destroy": (C.c_int, [_P]),
+    "mtr_geometry_from_tilts": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(XF), C.c_double, C.c_int, C.c_int,
+                                           VolumeSize, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "mtr_tlt_read": (C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int)]),
+    "mtr_xf_read": (C.c_int, [C.c_char_p, C.POINTER(XF), C.c_int, C.POINTER(C.c_int)]),
     "mtr_server_create": (C.c_int, [_P, C.c_longlong, C.c_int, C.POINTER(_P)]),
     "mtr_server_submit": (C.c_int, [_P, C.POINTER(RequestC), C.POINTER(C.c_longlong)]),
     "mtr_server_step": (C.c_int, [_P, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_int)]),
@@ -535,6 +543,39 @@ def parse_options(argv: Sequence[str]) -> tuple[int, OptionsC]:
     o = OptionsC()
     st = load().mtr_parse_options(len(args), arr, C.byref(o))
     return st, o
+
+
+def geometry_from_tilts(tilt_deg, phi_deg: float, det_x: int, det_y: int, vol: VolumeSize,
+                        xf=None) -> tuple[np.ndarray, np.ndarray]:
+    """Per-view linear maps (x_coef, y_coef), [4*n] each, of a tilt series
+    about an axis at in-plane angle phi; xf: optional [n, 6] alignment rows
+    (a11 a12 a21 a22 dx dy) mapping raw view coordinates to aligned ones."""
+    t = np.ascontiguousarray(tilt_deg, np.float64).reshape(-1)
+    n = len(t)
+    xs, ys = np.empty(4 * n), np.empty(4 * n)
+    dp = C.POINTER(C.c_double)
+    xfa = None
+    if xf is not None:
+        x = np.ascontiguousarray(xf, np.float64).reshape(n, 6)
+        xfa = (XF * n)(*[XF(*row) for row in x])
+    _check(load().mtr_geometry_from_tilts(n, t.ctypes.data_as(dp), xfa, float(phi_deg), det_x, det_y, vol,
+                                          xs.ctypes.data_as(dp), ys.ctypes.data_as(dp)), "mtr_geometry_from_tilts")
+    return xs, ys
+
+
+def read_tlt(path: str, cap: int = 100000) -> np.ndarray:
+    out = np.empty(cap, np.float64)
+    n = C.c_int()
+    _check(load().mtr_tlt_read(str(path).encode(), out.ctypes.data_as(C.POINTER(C.c_double)), cap, C.byref(n)),
+           "mtr_tlt_read")
+    return out[:n.value].copy()
+
+
+def read_xf(path: str, cap: int = 100000) -> np.ndarray:
+    arr = (XF * cap)()
+    n = C.c_int()
+    _check(load().mtr_xf_read(str(path).encode(), arr, cap, C.byref(n)), "mtr_xf_read")
+    return np.array([[getattr(arr[i], f) for f, _ in XF._fields_] for i in range(n.value)], np.float64).reshape(-1, 6)
 
 
 def estimate_footprint(prjs: Sequence[tuple[int, int, int]], vol: VolumeSize, precision: int) -> int:
