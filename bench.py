@@ -54,8 +54,8 @@ CONFIGS = {
 # Per-launch DRAM traffic and instruction count of the dominant kernel, from
 # the ncu captures summarised in profiles/ (one launch of axis 0).
 NCU_PROFILES = {
-    ("c2", "backproject"): {"traffic": 330_938_368 + 157_545_984, "warp_inst": 1_426_398_948,
-                            "duration_ms": 1.371552, "sm_ghz": 2.07, "sms": 152,
+    ("c2", "backproject"): {"traffic": 331_134_208 + 161_469_952, "warp_inst": 1_384_493_196,
+                            "duration_ms": 1.272832, "sm_ghz": 2.065, "sms": 152,
                             "source": "profiles/bp_tma_kernel_3axis_512x512x128.md"},
 }
 

@@ -206,6 +206,26 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
 mtr_status mtr_recon_upload(mtr_recon* r, int axis, const float* prj_data, int mem_kind);
 /* WBP init + MACE loop on the device (asynchronous on the context stream). */
 mtr_status mtr_recon_run(mtr_recon* r);
+/* The same run in pieces, and checkpoint/resume of the MACE state between
+ * outer iterations.  No counterpart in the reference (its checkpoint code is
+ * commented out, MultiAxis.cpp:208-214).
+ *   mtr_recon_init      WBP init (asynchronous);
+ *   mtr_recon_run_outer MACE outer iterations [first, first + count)
+ *                       (asynchronous);
+ *   mtr_recon_save      synchronises and writes w_avg, every w_k and the
+ *                       number of outer iterations done;
+ *   mtr_recon_load      recomputes the geometry sums (WBP init), then
+ *                       restores the saved state and z_k = 2 w_avg - w_k;
+ *                       *outer_done tells where to continue.  A file of
+ *                       another volume or axis count is
+ *                       MTR_ERR_INVALID_ARGUMENT, a damaged one MTR_ERR_FORMAT.
+ * init + run_outer(0, n) is mtr_recon_run; a run resumed from a checkpoint
+ * after outer iteration i equals the uninterrupted run up to the order of
+ * floating-point additions in the forward splat. */
+mtr_status mtr_recon_init(mtr_recon* r);
+mtr_status mtr_recon_run_outer(mtr_recon* r, int first, int count);
+mtr_status mtr_recon_save(mtr_recon* r, const char* path);
+mtr_status mtr_recon_load(mtr_recon* r, const char* path, int* outer_done);
 /* Copy w_avg out (host or device destination); synchronises for host. */
 mtr_status mtr_recon_download(mtr_recon* r, float* out, int mem_kind);
 /* Synchronises and reports MTR_ERR_TIMEOUT if a kernel of the last run gave

@@ -203,6 +203,7 @@ struct mtr_recon {
   mtr::DevBuf err;        // device error flag written by bounded waits (int)
   long long bytes = 0;
   bool geometry_ready = false;  // cf and cbp computed
+  int outer_done = 0;           // MACE outer iterations the state has been through
   cudaGraphExec_t graph = nullptr;
   long long graph_nodes = 0;
   ~mtr_recon();

@@ -10,9 +10,13 @@
 // and each MACE iteration ends with one fused launch over all axes.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <new>
+#include <string>
+#include <vector>
 
 #include "mtr_internal.h"
 #include "mtr_runtime.h"
@@ -214,29 +218,43 @@ mtr_status mtr::recon_enqueue_sirt_bp(mtr_recon* r, int k) { return enqueue_bp(r
 
 namespace {
 
-// WBP init, then the MACE loop.
-mtr_status enqueue_run(mtr_recon* r) {
-  mtr_status st = recon_enqueue_init(r);
-  if (st != MTR_OK) return st;
+// MACE outer iterations [first, first + count): n_inner SIRT iterations of
+// every axis, then the MACE step.
+mtr_status enqueue_outer(mtr_recon* r, int first, int count) {
   const int K = r->K, ni = r->p.sirt_inner, no = r->p.iter_times;
   double* norms = r->norms.as<double>();
-  for (int it = 0; it < no; ++it) {
+  for (int it = first; it < first + count; ++it) {
     for (int k = 0; k < K; ++k) {
       AxisState& a = r->ax[k];
       for (int j = 0; j < ni; ++j) {
         mtr_status s = enqueue_forward(r, a);
         if (s != MTR_OK) return s;
-        s = enqueue_residual(r, a, norms ? norms + ((long long)it * K + k) * ni + j : nullptr);
+        s = enqueue_residual(r, a, norms && it < no ? norms + ((long long)it * K + k) * ni + j : nullptr);
         if (s != MTR_OK) return s;
         s = enqueue_bp(r, a, 1, nullptr);
         if (s != MTR_OK) return s;
       }
     }
-    st = recon_enqueue_mace(r, it);
+    mtr_status st = recon_enqueue_mace(r, it);
     if (st != MTR_OK) return st;
   }
   return MTR_OK;
 }
+
+// WBP init, then the MACE loop.
+mtr_status enqueue_run(mtr_recon* r) {
+  mtr_status st = recon_enqueue_init(r);
+  if (st != MTR_OK) return st;
+  return enqueue_outer(r, 0, r->p.iter_times);
+}
+
+// Checkpoint file: header, then w_avg and w_k of every axis (float32, x fastest).
+struct CkptHeader {
+  char magic[8];  // "MTRCKPT1"
+  int32_t version, K, X, Y, Z, outer_done, precision;
+  int64_t reserved;
+};
+constexpr char kCkptMagic[8] = {'M', 'T', 'R', 'C', 'K', 'P', 'T', '1'};
 
 }  // namespace
 
@@ -366,10 +384,112 @@ mtr_status mtr_recon_upload(mtr_recon* r, int axis, const float* prj_data, int m
   return upload_projections(r, axis, prj_data, mem_kind);
 }
 
+mtr_status mtr_recon_init(mtr_recon* r) {
+  if (!r) return MTR_ERR_INVALID_ARGUMENT;
+  DeviceGuard g(r->ctx->device);
+  r->outer_done = 0;
+  return recon_enqueue_init(r);
+}
+
+mtr_status mtr_recon_run_outer(mtr_recon* r, int first, int count) {
+  if (!r || first < 0 || count < 0) return MTR_ERR_INVALID_ARGUMENT;
+  DeviceGuard g(r->ctx->device);
+  mtr_status s = enqueue_outer(r, first, count);
+  if (s == MTR_OK) r->outer_done = first + count;
+  return s;
+}
+
+mtr_status mtr_recon_save(mtr_recon* r, const char* path) {
+  if (!r || !path) return MTR_ERR_INVALID_ARGUMENT;
+  mtr_context* ctx = r->ctx;
+  DeviceGuard g(ctx->device);
+  const size_t vb = (size_t)r->nv * 4;
+  std::vector<float> host((size_t)r->nv);
+  CkptHeader h{};
+  std::memcpy(h.magic, kCkptMagic, 8);
+  h.version = 1;
+  h.K = r->K;
+  h.X = r->vs.X;
+  h.Y = r->vs.Y;
+  h.Z = r->vs.Z;
+  h.outer_done = r->outer_done;
+  h.precision = r->p.precision;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return set_error(ctx, MTR_ERR_IO, std::string("cannot create ") + path);
+  bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+  for (int k = -1; ok && k < r->K; ++k) {
+    const void* src = k < 0 ? r->wavg.p : r->ax[k].w.p;
+    cudaError_t e = cudaMemcpyAsync(host.data(), src, vb, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+      std::fclose(f);
+      return cuda_error(ctx, e, "checkpoint download");
+    }
+    ok = std::fwrite(host.data(), 4, (size_t)r->nv, f) == (size_t)r->nv;
+  }
+  ok = (std::fclose(f) == 0) && ok;
+  if (!ok) return set_error(ctx, MTR_ERR_IO, std::string("cannot write ") + path);
+  return mtr_recon_check(r);
+}
+
+mtr_status mtr_recon_load(mtr_recon* r, const char* path, int* outer_done) {
+  if (!r || !path) return MTR_ERR_INVALID_ARGUMENT;
+  mtr_context* ctx = r->ctx;
+  DeviceGuard g(ctx->device);
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return set_error(ctx, MTR_ERR_IO, std::string("cannot open ") + path);
+  CkptHeader h{};
+  if (std::fread(&h, sizeof h, 1, f) != 1 || std::memcmp(h.magic, kCkptMagic, 8) != 0 || h.version != 1) {
+    std::fclose(f);
+    return set_error(ctx, MTR_ERR_FORMAT, "not a checkpoint file");
+  }
+  if (h.K != r->K || h.X != r->vs.X || h.Y != r->vs.Y || h.Z != r->vs.Z || h.outer_done < 0) {
+    std::fclose(f);
+    return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "checkpoint of another volume or axis count");
+  }
+  // the WBP init computes the back-projection weight sums the SIRT update
+  // reads; its volumes are then replaced by the saved state
+  mtr_status s = recon_enqueue_init(r);
+  if (s != MTR_OK) {
+    std::fclose(f);
+    return s;
+  }
+  const size_t vb = (size_t)r->nv * 4;
+  std::vector<float> host((size_t)r->nv);
+  for (int k = -1; k < r->K; ++k) {
+    if (std::fread(host.data(), 4, (size_t)r->nv, f) != (size_t)r->nv) {
+      std::fclose(f);
+      return set_error(ctx, MTR_ERR_FORMAT, "truncated checkpoint");
+    }
+    void* dst = k < 0 ? r->wavg.p : r->ax[k].w.p;
+    cudaError_t e = cudaMemcpyAsync(dst, host.data(), vb, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // host buffer is reused
+    if (e != cudaSuccess) {
+      std::fclose(f);
+      return cuda_error(ctx, e, "checkpoint upload");
+    }
+  }
+  std::fclose(f);
+  // next SIRT start z_k = 2 w_avg - w_k (as the MACE step leaves it) and its copy
+  const int ck = copy_kind_of(r->p.precision);
+  for (auto& a : r->ax) {
+    launch_initial_z(a.w.as<float>(), r->wavg.as<float>(), a.x.as<float>(), r->nv, ctx->stream);
+    MTR_CK_LAUNCH(ctx, "resume z");
+    if (ck) {
+      launch_convert_copy(a.x.as<float>(), a.xcopy.p, ck, r->nv, ctx->stream);
+      MTR_CK_LAUNCH(ctx, "resume copy");
+    }
+  }
+  r->outer_done = h.outer_done;
+  if (outer_done) *outer_done = h.outer_done;
+  return MTR_OK;
+}
+
 mtr_status mtr_recon_run(mtr_recon* r) {
   if (!r) return MTR_ERR_INVALID_ARGUMENT;
   mtr_context* ctx = r->ctx;
   DeviceGuard g(ctx->device);
+  r->outer_done = r->p.iter_times;
   if (!(r->p.flags & MTR_FLAG_GRAPH)) return enqueue_run(r);
   if (!r->graph) {
     cudaGraph_t graph = nullptr;

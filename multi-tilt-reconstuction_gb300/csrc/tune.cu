@@ -94,8 +94,9 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
     if (a.hyc[4 * k + 3] != 0.0) bz0 = false;
   }
   char buf[256];
-  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d", a.PX, a.PY, a.A,
-                v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
+  // the trailing tag names the timing method, so choices cached by an older one are not reused
+  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t2", a.PX, a.PY,
+                a.A, v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
   return buf;
 }
 
@@ -173,6 +174,10 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
   }
   const int z0 = v.Zs, z1 = v.Zs + v.NZ;
   if (!known && autotune_enabled()) {
+    // Non-zero weight sums, so that every candidate's SIRT epilogue reads and
+    // writes the volume as a real run does (with zeros it would skip the
+    // update, hiding the cost of strided lanes-along-Y stores).
+    launch_fill(scratch_cbp, (long long)v.NX * v.NY * v.NZ, 1.f, ctx->stream);
     // back-projection candidates: depth x lane axis
     std::vector<std::function<cudaError_t()>> cands;
     std::vector<std::pair<int, int>> what;

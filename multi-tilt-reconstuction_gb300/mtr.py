@@ -135,6 +135,10 @@ _SIGNATURES = {
                                    C.POINTER(_P)]),
     "mtr_recon_upload": (C.c_int, [_P, C.c_int, _P, C.c_int]),
     "mtr_recon_run": (C.c_int, [_P]),
+    "mtr_recon_init": (C.c_int, [_P]),
+    "mtr_recon_run_outer": (C.c_int, [_P, C.c_int, C.c_int]),
+    "mtr_recon_save": (C.c_int, [_P, C.c_char_p]),
+    "mtr_recon_load": (C.c_int, [_P, C.c_char_p, C.POINTER(C.c_int)]),
     "mtr_recon_download": (C.c_int, [_P, _P, C.c_int]),
     "mtr_recon_download_axes": (C.c_int, [_P, _P, C.c_int]),
     "mtr_recon_check": (C.c_int, [_P]),
@@ -370,6 +374,21 @@ class Recon:
         buf = C.create_string_buffer(8192)
         self.ctx.check(self.ctx.lib.mtr_recon_describe(self.h, buf, len(buf)), "describe")
         return json.loads(buf.value.decode())
+
+    def init(self) -> None:
+        self.ctx.check(self.ctx.lib.mtr_recon_init(self.h), "mtr_recon_init")
+
+    def run_outer(self, first: int, count: int) -> None:
+        self.ctx.check(self.ctx.lib.mtr_recon_run_outer(self.h, first, count), "mtr_recon_run_outer")
+
+    def save(self, path) -> None:
+        self.ctx.check(self.ctx.lib.mtr_recon_save(self.h, str(path).encode()), "mtr_recon_save")
+
+    def load(self, path) -> int:
+        """Restore a checkpoint; returns the outer iterations it had done."""
+        n = C.c_int()
+        self.ctx.check(self.ctx.lib.mtr_recon_load(self.h, str(path).encode(), C.byref(n)), "mtr_recon_load")
+        return n.value
 
     def footprint(self) -> int:
         b = C.c_longlong()
