@@ -57,7 +57,6 @@ struct BpArgs {
 
 template <typename PT> __device__ __forceinline__ float to_f(PT v);
 template <> __device__ __forceinline__ float to_f<float>(float v) { return v; }
-template <> __device__ __forceinline__ float to_f<__half>(__half v) { return __half2float(v); }
 
 __device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 
@@ -97,6 +96,30 @@ __device__ __forceinline__ void bp_column(float (&s)[NZ], const PT* row0, int WX
   }
 }
 
+// The same column gather from a row pre-blended by the warp: b[i] holds the
+// y-interpolated detector value at window column i, so a voxel needs 2 taps.
+template <bool ASC, int NZ>
+__device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float* b, float xr, float a3, int lxm) {
+  constexpr int zf = ASC ? 0 : NZ - 1;
+  const float x = fmaf(a3, (float)zf, xr);
+  const float flx = floorf(x);
+  float fx = x - flx;
+  const float step = fabsf(a3);
+  const float* p = b + (magic_int(flx) + lxm);
+#pragma unroll
+  for (int i = 0; i < NZ; ++i) {
+    const int z = ASC ? i : NZ - 1 - i;
+    if (i > 0) {
+      fx += step;
+      const bool adv = fx >= 1.f;
+      fx = adv ? fx - 1.f : fx;
+      p += adv ? 1 : 0;
+    }
+    const float p0 = p[0], p1 = p[1];
+    s[z] += fmaf(fx, p1 - p0, p0);
+  }
+}
+
 // One brick (bx, by, bz) of one axis.  LANE_Y: consecutive lanes walk Y (used
 // when the detector x follows Y).  `smem` is the CTA's dynamic shared memory;
 // `reinit` re-initialises the mbarriers of a CTA that already ran a brick.
@@ -113,6 +136,8 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   const int win_elems = P.WX * P.WY;
   const size_t stage_bytes = (((size_t)win_elems * sizeof(PT)) + 127) & ~(size_t)127;
   PT* win0 = reinterpret_cast<PT*>(smem + 128 + kc_bytes);
+  // per-warp blended row (uniform-row angles of the SIRT update)
+  float* blend = reinterpret_cast<float*>(smem + 128 + kc_bytes + NST * stage_bytes) + (threadIdx.x >> 5) * P.WX;
 
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
@@ -197,14 +222,35 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 
   for (int a = 0; a < A; ++a) {
     const int st = a % NST;
-    if (!mbar_wait_bounded(&full[st], (uint32_t)((a / NST) & 1), kWaitIters)) {
-      atomicExch(P.err, 4);
+    // every lane of the warp takes the same branch (the warp syncs below)
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(&full[st], (uint32_t)((a / NST) & 1), kWaitIters))) {
+      if (lane == 0) atomicExch(P.err, 4);
       break;
     }
     const PT* w = reinterpret_cast<const PT*>(reinterpret_cast<const unsigned char*>(win0) + st * stage_bytes);
     const WinConst k = kc[a];
     const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
-    const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
+    float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
+    // Uniform rows: the detector y does not move along the lanes (|slope| * 31
+    // below 1e-6 px), so every lane of the warp reads the same two rows with
+    // the same weights; the warp blends them once per angle.
+    const bool uni = BZ0 && MODE == 1 && fabsf(LANE_Y ? k.b2 : k.b1) < 3e-8f;
+    bool blended = false;
+    if (uni) {
+      yr = __shfl_sync(0xffffffffu, yr, 0);
+      const float fly = floorf(yr);
+      const float fy = yr - fly;
+      const int rowi = magic_int(fly) + k.lym;
+      if ((unsigned)rowi < lim_y) {
+        const PT* row0 = w + rowi * WX;
+        for (int i = lane; i < WX; i += 32) {
+          const float r0 = to_f(row0[i]);
+          blend[i] = fmaf(fy, to_f(row0[i + WX]) - r0, r0);
+        }
+        blended = true;
+      }
+      __syncwarp();
+    }
     bool done = !active;
     if (active && BZ0 && MODE == 1 && fabsf(k.a3) < 0.999f) {
       // x is affine in z: the column's end voxels bound every tap index, so
@@ -216,9 +262,14 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
       const int ixa = magic_int(floorf(xr)) + k.lxm;
       const int ixb = magic_int(floorf(fmaf(k.a3, (float)(NZ - 1), xr))) + k.lxm;
       if ((unsigned)rowi < lim_y && (unsigned)min(ixa, ixb) < lim_x && (unsigned)(max(ixa, ixb) + 1) < lim_x) {
-        const PT* row0 = w + rowi * WX;
-        if (k.a3 >= 0.f) bp_column<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
-        else bp_column<false, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+        if (blended) {
+          if (k.a3 >= 0.f) bp_column_blended<true, NZ>(s, blend, xr, k.a3, k.lxm);
+          else bp_column_blended<false, NZ>(s, blend, xr, k.a3, k.lxm);
+        } else {
+          const PT* row0 = w + rowi * WX;
+          if (k.a3 >= 0.f) bp_column<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+          else bp_column<false, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+        }
         done = true;
       }
     }
@@ -309,7 +360,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 // bricks of the same rows at all depths run together, so the detector rows
 // they read stay in L2 instead of being re-read from DRAM once per z layer.
 template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, MODE == 1 ? 5 : 4)
 bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
   bp_brick<PT, MODE, LANE_Y, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
@@ -440,7 +491,8 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
   p.WY = (int)std::ceil(ey) + 4;
   p.ok = p.WX <= 256 && p.WY <= 256 && (nz == 4 || nz == 8 || nz == 16);
   const size_t stage = (((size_t)p.WX * p.WY * (half ? 2 : 4)) + 127) & ~(size_t)127;
-  p.smem = 128 + ((((size_t)A * sizeof(WinConst)) + 127) & ~(size_t)127) + NST * stage;
+  p.smem = 128 + ((((size_t)A * sizeof(WinConst)) + 127) & ~(size_t)127) + NST * stage +
+           (((size_t)kConsumerWarps * p.WX * sizeof(float) + 127) & ~(size_t)127);  // per-warp blended rows
   if (p.smem > 227 * 1024) p.ok = false;
   return p;
 }

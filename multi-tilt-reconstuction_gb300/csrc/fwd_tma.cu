@@ -120,6 +120,37 @@ __device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)
   atomicAdd(row + WX + cur + 1, fixq(wy1, acc1));
 }
 
+// stream_column for a warp whose lanes all splat into the same two detector
+// rows with the same y weights: the column emits its unsplit fixed-point
+// values into the warp's own row buffer `u` (one atomic per pixel instead of
+// two); the warp splits that row into the two detector rows afterwards.
+template <bool ASC, int NZ>
+__device__ __forceinline__ void stream_column_row(int* u, const float (&v)[NZ], float xr, float a3, int lxm) {
+  constexpr int zf = ASC ? 0 : NZ - 1;
+  const float x = fmaf(a3, (float)zf, xr);
+  const float flx = floorf(x);
+  float fx = x - flx;
+  const float step = fabsf(a3);
+  int cur = magic_int(flx) + lxm;
+  float acc0 = (1.f - fx) * v[zf], acc1 = fx * v[zf];
+#pragma unroll
+  for (int i = 1; i < NZ; ++i) {
+    const int z = ASC ? i : NZ - 1 - i;
+    fx += step;
+    if (fx >= 1.f) {
+      fx -= 1.f;
+      atomicAdd(u + cur, fixq(1.f, acc0));
+      acc0 = acc1;
+      acc1 = 0.f;
+      ++cur;
+    }
+    acc0 = fmaf(1.f - fx, v[z], acc0);
+    acc1 = fmaf(fx, v[z], acc1);
+  }
+  atomicAdd(u + cur, fixq(1.f, acc0));
+  atomicAdd(u + cur + 1, fixq(1.f, acc1));
+}
+
 // One brick (bx, by, zb) and angle group g of one axis; `smem` is the CTA's
 // dynamic shared memory.  On return every bulk reduce it issued is complete.
 template <typename VT, bool LANE_Y, bool BZ0, int NZ>
@@ -134,6 +165,9 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
   const size_t stage_bytes = ((size_t)win_elems * 4 + 127) & ~(size_t)127;
   unsigned char* win0 = smem + kc_bytes + 128;
   float* red = reinterpret_cast<float*>(smem + kc_bytes);  // 32 floats for the block max
+  // per-warp row buffers of the uniform-row angles (kept zero between uses)
+  int* urow = reinterpret_cast<int*>(win0 + 2 * stage_bytes) + (threadIdx.x >> 5) * WX;
+  for (int i = threadIdx.x & 31; i < WX; i += 32) urow[i] = 0;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int A = P.ax.A;
@@ -225,7 +259,31 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
     }
     __syncthreads();
     const FwdConst k = kc[j];
-    if (active && BZ0 && k.interior && fabsf(k.a3) < 0.999f) {
+    // Uniform rows: the detector y does not move along the lanes (|slope| * 31
+    // below 1e-6 px), so the lanes of a warp share their two rows and weights.
+    if (BZ0 && k.interior && fabsf(k.a3) < 0.999f && fabsf(LANE_Y ? k.b2 : k.b1) < 3e-8f) {
+      const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
+      const float yr = __shfl_sync(0xffffffffu, fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf)), 0);
+      if (active) {
+        if (k.a3 >= 0.f) stream_column_row<true, NZ>(urow, v, xr, k.a3, k.lxm);
+        else stream_column_row<false, NZ>(urow, v, xr, k.a3, k.lxm);
+      }
+      __syncwarp();
+      // split the warp's row into the two detector rows (values up to 2^30:
+      // rounded with a conversion, the magic-number rounding needs < 2^22)
+      const float fly = floorf(yr);
+      const float fy = yr - fly;
+      int* rowp = wi + (magic_int(fly) + k.lym) * WX;
+      for (int i = lane; i < WX; i += 32) {
+        const int q = urow[i];
+        if (q != 0) {
+          const float uf = (float)q;
+          atomicAdd(rowp + i, __float2int_rn((1.f - fy) * uf));
+          atomicAdd(rowp + WX + i, __float2int_rn(fy * uf));
+          urow[i] = 0;
+        }
+      }
+    } else if (active && BZ0 && k.interior && fabsf(k.a3) < 0.999f) {
       // every tap lands in the window and on the detector; stream the column
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
       const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
@@ -461,7 +519,9 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
   p.WY = (int)std::ceil(ey) + 4;
   const size_t stage = (((size_t)p.WX * p.WY * 4) + 127) & ~(size_t)127;
   // constants for up to A angles (one group) + block-max scratch + 2 stages
-  p.smem = ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 128 + 2 * stage;
+  // + per-warp row buffers of the uniform-row angles
+  p.smem = ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 128 + 2 * stage +
+           (size_t)kWarps * p.WX * sizeof(int);
   // Weight a pixel can receive from one brick: per Z plane at most the number
   // of voxels whose taps reach it, i.e. lattice points in the preimage of a
   // 2x2-pixel square under the in-plane map J (bounding box of J^-1 [-1,1]^2).
