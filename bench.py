@@ -173,6 +173,39 @@ def make_inputs(cfg: dict, device: str):
     return vol, axes, case["meta"]
 
 
+def mrc_load_throughput(torch, mtr, ctx, data: np.ndarray) -> dict:
+    """Axis 0 written as an int16 MRC stack (scaled to +-30000), then loaded
+    into device memory twice: the host reader (float32 array) followed by a
+    copy to the device, and mtr_mrc_read_stack_device.  The file was just
+    written, so both read it from the page cache."""
+    import tempfile
+
+    d = tempfile.mkdtemp(prefix="mtr_io_")
+    path = os.path.join(d, "axis0.mrc")
+    try:
+        scale = 30000.0 / max(float(np.abs(data).max()), 1e-30)
+        mtr.write_mrc_stack(path, data * scale, 1)
+        nbytes = data.size * 2
+        dev = torch.empty(data.size, dtype=torch.float32, device="cuda")
+        out = {"file_bytes": nbytes, "mode": 1}
+        for name, fn in (("host_read_then_copy", lambda: dev.copy_(torch.from_numpy(mtr.read_mrc_stack(path).reshape(-1)))),
+                         ("device_read", lambda: mtr.read_mrc_stack_device(ctx, path, dev))):
+            fn()  # warm the page cache and the code path
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for _ in range(3):
+                fn()
+            torch.cuda.synchronize()
+            out[name + "_gbs"] = 3 * nbytes / (time.perf_counter() - t) / 1e9
+        out["speedup"] = out["device_read_gbs"] / out["host_read_then_copy_gbs"]
+        del dev
+        return out
+    finally:
+        if os.path.exists(path):
+            os.remove(path)
+        os.rmdir(d)
+
+
 def time_steps(torch, stream, recon, steps: int) -> float:
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
@@ -304,6 +337,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
             arr_ms.append(dt * 1e3)
     e2e_ms = max_over_ranks(statistics.mean(arr_ms))
 
+    io = mrc_load_throughput(torch, mtr, ctx, host_axes[0].data)
+
     # error of both paths against the all-FP64 GPU reconstruction of the same inputs
     err64 = None
     if args.fp64 and args.config != "c3":
@@ -319,7 +354,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
            "prof": prof, "launches": launches, "gen_s": gen_s, "meta": meta, "vu": vu,
            "mixed_vs_fp32": float(np.linalg.norm(out_mixed.astype(np.float64) - out_fp32) /
                                   max(np.linalg.norm(out_fp32.astype(np.float64)), 1e-30)),
-           "axes_host": host_axes, "vol": vol, "prec": prec, "err64": err64}
+           "axes_host": host_axes, "vol": vol, "prec": prec, "err64": err64, "io": io}
     rec.close()
     if ref32 is not rec:
         ref32.close()
@@ -687,6 +722,7 @@ def main() -> int:
                     "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"],
                     "api": "mtr_reconstruct (host buffers, pinned)"},
             "gpu_launches": r["launches"],
+            "io": r["io"],
             "roofline": roof,
             "clocks": r["clk"],
         }

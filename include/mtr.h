@@ -360,6 +360,13 @@ mtr_status mtr_mrc_read_header(const char* path, mtr_mrc_header* out);
  * bytes of the file (the reference takes file_size - n*2 for every mode,
  * which is the same offset for 16-bit modes).  Modes 0,1,2,6,12. */
 mtr_status mtr_mrc_read_stack(const char* path, float* out, long long n);
+/* The same values written straight into device memory (d_out: n floats on
+ * the context's device).  No counterpart in the reference, which reads
+ * element by element with fread (MrcFileIOBaseFunction.cpp:40-46): the data
+ * block is read in 32 MiB chunks into two pinned buffers, and each chunk is
+ * copied to the device and widened to float32 there while the next one is
+ * read.  Synchronises the context stream before returning. */
+mtr_status mtr_mrc_read_stack_device(mtr_context* ctx, const char* path, float* d_out, long long n);
 /* Replaces readCoef (MrcFileIOBaseFunction.cpp:72-134).  Appends x/y
  * coefficients (up to cap each), counts them in *n_x / *n_y, widens *vol by
  * the x->, y->, z-> bound lines and sets vol->X/Y/Z = end - start. */

@@ -164,6 +164,7 @@ _SIGNATURES = {
     "mtr_server_destroy": (C.c_int, [_P]),
     "mtr_mrc_read_header": (C.c_int, [C.c_char_p, C.POINTER(MrcHeader)]),
     "mtr_mrc_read_stack": (C.c_int, [C.c_char_p, _P, C.c_longlong]),
+    "mtr_mrc_read_stack_device": (C.c_int, [_P, C.c_char_p, _P, C.c_longlong]),
     "mtr_txbr_read": (C.c_int, [C.c_char_p, _P, _P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(VolumeSize)]),
     "mtr_volume_size_empty": (None, [C.POINTER(VolumeSize)]),
@@ -529,6 +530,12 @@ def read_mrc_stack(path: str) -> np.ndarray:
     out = np.empty((h.nz, h.ny, h.nx), np.float32)
     _check(load().mtr_mrc_read_stack(str(path).encode(), _ptr(out), out.size), "mtr_mrc_read_stack")
     return out
+
+
+def read_mrc_stack_device(ctx: "Context", path: str, out) -> None:
+    """Read an MRC stack's data into a CUDA float32 tensor `out` (numel = nx*ny*nz)."""
+    ctx.check(ctx.lib.mtr_mrc_read_stack_device(ctx.h, str(path).encode(), _ptr(out), out.numel()),
+              "mtr_mrc_read_stack_device")
 
 
 def read_txbr(path: str, cap: int, vol: VolumeSize | None = None):
