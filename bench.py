@@ -206,6 +206,11 @@ def mrc_load_throughput(torch, mtr, ctx, data: np.ndarray) -> dict:
         os.rmdir(d)
 
 
+def rel_l2_np(a, b) -> float:
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / max(np.linalg.norm(b), 1e-30))
+
+
 def time_steps(torch, stream, recon, steps: int) -> float:
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
@@ -303,6 +308,24 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     ms32 = time_steps(torch, stream, ref32, args.steps) if ref32 is not rec else ms
     ms32 = max_over_ranks(ms32)
 
+    # the plain FP32 path: the same library with its straightforward kernels
+    # (global-memory gather and global-atomic splat; MTR_DISABLE_TMA=1 is read
+    # at creation and at every launch, so it is set only around this run)
+    plain = None
+    if args.config in ("c1", "c2"):
+        os.environ["MTR_DISABLE_TMA"] = "1"
+        try:
+            rp = mtr.Recon(ctx, axes, vol, mk(mtr.PREC_FP32), mem_kind=mtr.MEM_DEVICE)
+            rp.run()
+            ms_plain = max_over_ranks(time_steps(torch, stream, rp, 1))
+            err_plain = rel_l2_np(rp.download(), ref32.download())
+            rp.close()
+        finally:
+            del os.environ["MTR_DISABLE_TMA"]
+        plain = {"ms_per_step": ms_plain, "mixed_over_plain": ms_plain / ms, "fp32_over_plain": ms_plain / ms32,
+                 "rel_l2_vs_fp32": err_plain,
+                 "kernels": "bp_gather_kernel + fwd_splat_kernel (global atomics), FP32"}
+
     out_mixed = rec.download()
     out_fp32 = ref32.download()
     # free both device-resident runs before the end-to-end calls allocate their own
@@ -354,7 +377,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
            "prof": prof, "launches": launches, "gen_s": gen_s, "meta": meta, "vu": vu,
            "mixed_vs_fp32": float(np.linalg.norm(out_mixed.astype(np.float64) - out_fp32) /
                                   max(np.linalg.norm(out_fp32.astype(np.float64)), 1e-30)),
-           "axes_host": host_axes, "vol": vol, "prec": prec, "err64": err64, "io": io}
+           "axes_host": host_axes, "vol": vol, "prec": prec, "err64": err64, "io": io, "plain": plain}
     rec.close()
     if ref32 is not rec:
         ref32.close()
@@ -717,6 +740,8 @@ def main() -> int:
                                   "tma": t["back_projection"]["tma"] and t["forward"]["tma"]} for t in r["tiles"]]},
             "fp32": {"value": vu / (r["ms32"] * 1e-3), "ms_per_step": r["ms32"],
                      "mixed_over_fp32": r["ms32"] / r["ms"]},
+            "plain_fp32": None if r["plain"] is None else {"value": vu / (r["plain"]["ms_per_step"] * 1e-3),
+                                                            **r["plain"]},
             "error": {"mixed_vs_fp32_rel_l2": r["mixed_vs_fp32"], **(r["err64"] or {})},
             "e2e": {"value": vu / (r["e2e_ms"] * 1e-3), "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"],

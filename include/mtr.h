@@ -235,6 +235,17 @@ mtr_status mtr_recon_check(mtr_recon* r);
 mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind);
 /* Squared residual norms, n_outer*K*n_inner doubles (MTR_FLAG_RECORD_NORMS). */
 mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n);
+/* FP64 convergence record of the MACE loop, computed on the GPU by the MACE
+ * step: out[it] = ||w_avg(it) - w_avg(it-1)|| / ||w_avg(it)||, the relative
+ * L2 change of the consensus in outer iteration it (w_avg(-1) = the WBP
+ * init), for the first min(n, n_outer) iterations (0 for iterations not run).
+ * The reference has no convergence test (fixed iteration counts,
+ * MultiAxis.cpp:45). */
+mtr_status mtr_recon_changes(mtr_recon* r, double* out, int n);
+/* Outer iterations from `first` until the relative change of the last one
+ * drops below tol or n_outer iterations are done; synchronises after each
+ * outer iteration.  *outer_done = outer iterations done. */
+mtr_status mtr_recon_run_until(mtr_recon* r, int first, double tol, int* outer_done);
 /* Device bytes held by the object. */
 mtr_status mtr_recon_footprint(const mtr_recon* r, long long* bytes);
 /* JSON description of the kernels and tile shapes chosen per axis (TMA

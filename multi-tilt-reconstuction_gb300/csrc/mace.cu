@@ -68,7 +68,8 @@ __global__ void widen_kernel(const __half* __restrict__ src, float* __restrict__
 //   wavg = (sum_k w[k]) / K      (summed in FP64)
 //   x[k] = 2 wavg - w[k]         (the next outer iteration's z_k)
 // and, when copy_kind != 0, x_copy[k] = x[k] in bf16/f16 for the forward pass.
-// dchange (optional) accumulates sum (wavg_new - wavg_old)^2 in FP64.
+// dchange (optional, 2 doubles) accumulates sum (wavg_new - wavg_old)^2 and
+// sum wavg_new^2 in FP64: the convergence test's relative change.
 constexpr int kMaxK = MTR_MAX_AXES;
 struct MacePtrs {
   float* w[kMaxK];
@@ -79,7 +80,7 @@ struct MacePtrs {
 __global__ void __launch_bounds__(kThreads)
 mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho, int copy_kind,
             double* __restrict__ dchange) {
-  double acc = 0.0;
+  double acc = 0.0, acc2 = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float wa = wavg[i];
     float wn[kMaxK];
@@ -98,6 +99,7 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
     wavg[i] = na;
     const double d = (double)na - (double)wa;
     acc += d * d;
+    acc2 += (double)na * (double)na;
 #pragma unroll
     for (int k = 0; k < kMaxK; ++k) {
       if (k < K) {
@@ -109,14 +111,24 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
     }
   }
   if (dchange) {
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    __shared__ double red[kThreads / 32];
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    for (int o = 16; o > 0; o >>= 1) {
+      acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      acc2 += __shfl_xor_sync(0xffffffffu, acc2, o);
+    }
+    __shared__ double red[2][kThreads / 32];
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = acc;
+      red[1][threadIdx.x >> 5] = acc2;
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int w = 0; w < kThreads / 32; ++w) t += red[w];
+      double t = 0.0, t2 = 0.0;
+      for (int w = 0; w < kThreads / 32; ++w) {
+        t += red[0][w];
+        t2 += red[1][w];
+      }
       atomicAdd(dchange, t);
+      atomicAdd(dchange + 1, t2);
     }
   }
 }

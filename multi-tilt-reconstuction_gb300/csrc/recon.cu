@@ -208,7 +208,7 @@ mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
   double* norms = r->norms.as<double>();
   double* dch = r->dchange.as<double>();
   if (norms) MTR_CK(ctx, cudaMemsetAsync(norms, 0, sizeof(double) * (size_t)no * K * ni, ctx->stream));
-  if (dch) MTR_CK(ctx, cudaMemsetAsync(dch, 0, sizeof(double) * (size_t)no, ctx->stream));
+  if (dch) MTR_CK(ctx, cudaMemsetAsync(dch, 0, sizeof(double) * 2 * (size_t)std::max(1, no), ctx->stream));
   return MTR_OK;
 }
 
@@ -274,7 +274,7 @@ mtr_status mtr::recon_enqueue_mace(mtr_recon* r, int it) {
   {
     ProfScope ps(ctx, MTR_KERNEL_MACE);
     launch_mace(K, ws, xs, r->wavg.as<float>(), r->nv, r->p.mace_step, xcs, copy_kind_of(r->p.precision),
-                dch && it < r->p.iter_times ? dch + it : nullptr, ctx->stream);
+                dch && it < r->p.iter_times ? dch + 2 * it : nullptr, ctx->stream);
   }
   MTR_CK_LAUNCH(ctx, "mace");
   return MTR_OK;
@@ -367,8 +367,10 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   if (params->flags & MTR_FLAG_RECORD_NORMS) {
     const size_t n = (size_t)std::max(1, params->iter_times) * n_axes * std::max(1, params->sirt_inner);
     MTR_CK(ctx, r->norms.alloc(sizeof(double) * n));
-    MTR_CK(ctx, r->dchange.alloc(sizeof(double) * std::max(1, params->iter_times)));
   }
+  // convergence record: FP64 sum (w_avg change)^2 and sum w_avg^2 per outer iteration
+  MTR_CK(ctx, r->dchange.alloc(sizeof(double) * 2 * std::max(1, params->iter_times)));
+  MTR_CK(ctx, cudaMemsetAsync(r->dchange.p, 0, sizeof(double) * 2 * std::max(1, params->iter_times), ctx->stream));
   s = enqueue_geometry(r.get());
   if (s != MTR_OK) return s;
   r->geometry_ready = true;
@@ -563,6 +565,36 @@ mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n) {
   MTR_CK(r->ctx, cudaMemcpyAsync(out, r->norms.p, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, r->ctx->stream));
   MTR_CK(r->ctx, cudaStreamSynchronize(r->ctx->stream));
   return MTR_OK;
+}
+
+mtr_status mtr_recon_changes(mtr_recon* r, double* out, int n) {
+  if (!r || !out || n < 0) return MTR_ERR_INVALID_ARGUMENT;
+  n = std::min(n, std::max(1, r->p.iter_times));
+  DeviceGuard g(r->ctx->device);
+  std::vector<double> raw(2 * (size_t)n);
+  MTR_CK(r->ctx, cudaMemcpyAsync(raw.data(), r->dchange.p, sizeof(double) * raw.size(), cudaMemcpyDeviceToHost,
+                                 r->ctx->stream));
+  MTR_CK(r->ctx, cudaStreamSynchronize(r->ctx->stream));
+  for (int i = 0; i < n; ++i) out[i] = raw[2 * i + 1] > 0.0 ? std::sqrt(raw[2 * i] / raw[2 * i + 1]) : 0.0;
+  return MTR_OK;
+}
+
+mtr_status mtr_recon_run_until(mtr_recon* r, int first, double tol, int* outer_done) {
+  if (!r || first < 0 || !(tol >= 0.0)) return MTR_ERR_INVALID_ARGUMENT;
+  DeviceGuard g(r->ctx->device);
+  int it = first;
+  while (it < r->p.iter_times) {
+    mtr_status s = enqueue_outer(r, it, 1);
+    if (s != MTR_OK) return s;
+    ++it;
+    r->outer_done = it;
+    std::vector<double> all((size_t)it);
+    s = mtr_recon_changes(r, all.data(), it);  // synchronises
+    if (s != MTR_OK) return s;
+    if (all[(size_t)it - 1] < tol) break;
+  }
+  if (outer_done) *outer_done = it;
+  return mtr_recon_check(r);
 }
 
 mtr_status mtr_recon_footprint(const mtr_recon* r, long long* bytes) {

@@ -143,6 +143,8 @@ _SIGNATURES = {
     "mtr_recon_download_axes": (C.c_int, [_P, _P, C.c_int]),
     "mtr_recon_check": (C.c_int, [_P]),
     "mtr_recon_norms": (C.c_int, [_P, C.POINTER(C.c_double), C.c_longlong]),
+    "mtr_recon_changes": (C.c_int, [_P, C.POINTER(C.c_double), C.c_int]),
+    "mtr_recon_run_until": (C.c_int, [_P, C.c_int, C.c_double, C.POINTER(C.c_int)]),
     "mtr_recon_footprint": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "mtr_recon_describe": (C.c_int, [_P, C.c_char_p, C.c_int]),
     "mtr_recon_destroy": (C.c_int, [_P]),
@@ -390,6 +392,18 @@ class Recon:
         n = C.c_int()
         self.ctx.check(self.ctx.lib.mtr_recon_load(self.h, str(path).encode(), C.byref(n)), "mtr_recon_load")
         return n.value
+
+    def changes(self, n: int) -> np.ndarray:
+        """Relative L2 change of the consensus per outer iteration (FP64)."""
+        out = np.zeros(n, np.float64)
+        self.ctx.check(self.ctx.lib.mtr_recon_changes(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), n),
+                       "mtr_recon_changes")
+        return out
+
+    def run_until(self, tol: float, first: int = 0) -> int:
+        done = C.c_int()
+        self.ctx.check(self.ctx.lib.mtr_recon_run_until(self.h, first, tol, C.byref(done)), "mtr_recon_run_until")
+        return done.value
 
     def footprint(self) -> int:
         b = C.c_longlong()

@@ -76,3 +76,26 @@ def test_checkpoint_file_layout(ctx, tmp_path):
     n = c.vol.X * c.vol.Y * c.vol.Z
     assert body.size == n * (1 + len(c.axes))
     np.testing.assert_array_equal(body[:n].reshape(wavg.shape), wavg)
+
+
+def test_convergence_record_and_early_stop(ctx):
+    """mtr_recon_changes is the relative L2 change of the consensus per outer
+    iteration (FP64 on the GPU); mtr_recon_run_until stops on it."""
+    c = cases.get("two_axis")
+    p = mtr.params(iter_times=4, sirt_inner=3, sirt_step=0.5, mace_step=0.8)
+    r = mtr.Recon(ctx, c.axes, c.vol, p)
+    r.init()
+    vols = [r.download().astype(np.float64)]  # the WBP init consensus
+    for it in range(4):
+        r.run_outer(it, 1)
+        vols.append(r.download().astype(np.float64))
+    ch = r.changes(4)
+    want = [np.linalg.norm(vols[i + 1] - vols[i]) / np.linalg.norm(vols[i + 1]) for i in range(4)]
+    np.testing.assert_allclose(ch, want, rtol=1e-9)
+    assert ch[0] > ch[1] > ch[2]
+    r.close()
+    for tol, expect in ((0.0, 4), (1e9, 1), (ch[1] * 1.001, 2)):
+        r2 = mtr.Recon(ctx, c.axes, c.vol, p)
+        r2.init()
+        assert r2.run_until(tol) == expect
+        r2.close()
