@@ -97,11 +97,12 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
       // brick depth, lane axis, windows and tensor maps as tuned for this axis
       const BpPlan& bp = a.plan;
       const FwdPlan& fp = a.fplan;
-      const int bgx = (v.NX + (bp.lane_y ? 8 : 32) - 1) / (bp.lane_y ? 8 : 32);
-      const int bgy = (v.NY + (bp.lane_y ? 32 : 8) - 1) / (bp.lane_y ? 32 : 8);
+      const int bgx = (v.NX + (bp.lanes == 1 ? 8 : 32) - 1) / (bp.lanes == 1 ? 8 : 32);
+      const int bgy = (v.NY + (bp.lanes == 1 ? 32 : 8) - 1) / (bp.lanes == 1 ? 32 : 8);
       const int fgx = (v.NX + (fp.lane_y ? 8 : 32) - 1) / (fp.lane_y ? 8 : 32);
       const int fgy = (v.NY + (fp.lane_y ? 32 : 8) - 1) / (fp.lane_y ? 32 : 8);
-      const bool bp_ok = a.tma && !tma_disabled() &&
+      // the persistent kernel takes lines along X or Y; patch-tiled axes keep their own launches
+      const bool bp_ok = a.tma && !tma_disabled() && bp.lanes != 2 &&
                          (long long)bgx * bgy * ((v.NZ + bp.nz - 1) / bp.nz) <
                              (long long)kOwnWaves * ctx->num_sms * backproject_batch_ctas_per_sm(bp.smem);
       const bool fwd_ok = a.ftma && !tma_disabled() &&
@@ -115,10 +116,10 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
         d.ax = a.dev();
         d.vol = v;
         d.WX = bp.WX; d.WY = bp.WY; d.align = bp.align;
-        const int BX = bp.lane_y ? 8 : 32, BY = bp.lane_y ? 32 : 8;
+        const int BX = bp.lanes == 1 ? 8 : 32, BY = bp.lanes == 1 ? 32 : 8;
         d.gx = (v.NX + BX - 1) / BX;
         d.gy = (v.NY + BY - 1) / BY;
-        d.lane_y = bp.lane_y; d.bz0 = bp.bz0; d.nz = bp.nz;
+        d.lane_y = bp.lanes == 1; d.bz0 = bp.bz0; d.nz = bp.nz;
         d.step = r->p.sirt_step;
         d.vol_out = a.x.as<float>();
         d.cbp = a.cbp.as<float>();

@@ -120,14 +120,18 @@ __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float* b
   }
 }
 
-// One brick (bx, by, bz) of one axis.  LANE_Y: consecutive lanes walk Y (used
-// when the detector x follows Y).  `smem` is the CTA's dynamic shared memory;
-// `reinit` re-initialises the mbarriers of a CTA that already ran a brick.
-template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
+// One brick (bx, by, bz) of one axis.  LANES: 0 = each warp a line of 32
+// voxels along X (brick 32x8), 1 = a line along Y (brick 8x32, used when the
+// detector x follows Y), 2 = an 8x4 patch (brick 32x8: on oblique axes the
+// taps of a line fall on a diagonal of the window that maps several lanes to
+// one shared-memory bank; a patch keeps them compact).  `smem` is the CTA's
+// dynamic shared memory; `reinit` re-initialises the mbarriers of a CTA that
+// already ran a brick.
+template <typename PT, int MODE, int LANES, bool BZ0, int NZ>
 __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& P, int bx, int by, int bz,
                                          unsigned char* smem, bool reinit) {
-  constexpr int BX = LANE_Y ? kConsumerWarps : 32;
-  constexpr int BY = LANE_Y ? 32 : kConsumerWarps;
+  constexpr int BX = LANES == 1 ? kConsumerWarps : 32;
+  constexpr int BY = LANES == 1 ? 32 : kConsumerWarps;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + NST;
   WinConst* kc = reinterpret_cast<WinConst*>(smem + 128);
@@ -210,8 +214,8 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   }
 
   // ---------------- consumer warps
-  const int tx = LANE_Y ? warp : lane;
-  const int ty = LANE_Y ? lane : warp;
+  const int tx = LANES == 0 ? lane : LANES == 1 ? warp : (warp & 3) * 8 + (lane & 7);
+  const int ty = LANES == 0 ? warp : LANES == 1 ? lane : (warp >> 2) * 4 + (lane >> 3);
   const bool active = (X0 + tx < P.vol.Xs + P.vol.NX) && (Y0 + ty < P.vol.Ys + P.vol.NY);
   const int WX = P.WX;
   const unsigned lim_x = (unsigned)(WX - 1), lim_y = (unsigned)(P.WY - 1);
@@ -234,7 +238,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
     // Uniform rows: the detector y does not move along the lanes (|slope| * 31
     // below 1e-6 px), so every lane of the warp reads the same two rows with
     // the same weights; the warp blends them once per angle.
-    const bool uni = BZ0 && MODE == 1 && fabsf(LANE_Y ? k.b2 : k.b1) < 3e-8f;
+    const bool uni = BZ0 && MODE == 1 && LANES != 2 && fabsf(LANES == 1 ? k.b2 : k.b1) < 3e-8f;
     bool blended = false;
     if (uni) {
       yr = __shfl_sync(0xffffffffu, yr, 0);
@@ -359,31 +363,35 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 // One CTA per brick of one axis.  The grid runs x fastest, then z, then y:
 // bricks of the same rows at all depths run together, so the detector rows
 // they read stay in L2 instead of being re-read from DRAM once per z layer.
-template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
+template <typename PT, int MODE, int LANES, bool BZ0, int NZ>
 __global__ void __launch_bounds__(kThreads, MODE == 1 ? 5 : 4)
 bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
-  bp_brick<PT, MODE, LANE_Y, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
+  bp_brick<PT, MODE, LANES, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
 }
 
-template <typename PT, int MODE, bool LANE_Y, bool BZ0, int NZ>
+template <typename PT, int MODE, int LANES, bool BZ0, int NZ>
 cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cudaStream_t st) {
-  auto kern = bp_tma_kernel<PT, MODE, LANE_Y, BZ0, NZ>;
+  auto kern = bp_tma_kernel<PT, MODE, LANES, BZ0, NZ>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int BX = LANE_Y ? kConsumerWarps : 32, BY = LANE_Y ? 32 : kConsumerWarps;
+  const int BX = LANES == 1 ? kConsumerWarps : 32, BY = LANES == 1 ? 32 : kConsumerWarps;
   const dim3 grid((P.vol.NX + BX - 1) / BX, (P.z1 - P.z0 + NZ - 1) / NZ, (P.vol.NY + BY - 1) / BY);
   kern<<<grid, kThreads, smem, st>>>(map, P);
   return cudaGetLastError();
 }
 
-template <typename PT, int MODE, bool LANE_Y, bool BZ0>
+template <typename PT, int MODE, int LANES, bool BZ0>
 cudaError_t launch_nz(const CUtensorMap& map, const BpArgs& P, const BpPlan& plan, cudaStream_t st) {
   // WBP runs once per reconstruction: one brick depth.  SIRT: the tuned depth.
-  if (MODE == 0 || plan.nz == 8) return launch_one<PT, MODE, LANE_Y, BZ0, 8>(map, P, plan.smem, st);
-  if (plan.nz == 4) return launch_one<PT, MODE, LANE_Y, BZ0, 4>(map, P, plan.smem, st);
-  if (plan.nz == 16) return launch_one<PT, MODE, LANE_Y, BZ0, 16>(map, P, plan.smem, st);
-  return cudaErrorInvalidValue;
+  if constexpr (MODE == 0) {
+    return launch_one<PT, 0, LANES, BZ0, 8>(map, P, plan.smem, st);
+  } else {
+    if (plan.nz == 8) return launch_one<PT, MODE, LANES, BZ0, 8>(map, P, plan.smem, st);
+    if (plan.nz == 4) return launch_one<PT, MODE, LANES, BZ0, 4>(map, P, plan.smem, st);
+    if (plan.nz == 16) return launch_one<PT, MODE, LANES, BZ0, 16>(map, P, plan.smem, st);
+    return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace
@@ -401,11 +409,11 @@ namespace {
 template <int NZ>
 __device__ __forceinline__ void bp_batch_item(const CUtensorMap* map, const BpArgs& P, const int* b,
                                               unsigned char* smem, bool reinit) {
-  switch (b[4]) {
-    case 0: bp_brick<float, 1, false, false, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
-    case 1: bp_brick<float, 1, false, true, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
-    case 2: bp_brick<float, 1, true, false, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
-    default: bp_brick<float, 1, true, true, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+  switch (b[4]) {  // lines along X or Y (axes tuned to patches keep their own launches)
+    case 0: bp_brick<float, 1, 0, false, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+    case 1: bp_brick<float, 1, 0, true, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+    case 2: bp_brick<float, 1, 1, false, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
+    default: bp_brick<float, 1, 1, true, NZ>(map, P, b[0], b[1], b[2], smem, reinit); break;
   }
 }
 
@@ -461,6 +469,54 @@ cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const long long* 
   return cudaGetLastError();
 }
 
+namespace {
+
+// Mean number of shared-memory wavefronts per tap load of one warp for a
+// window row pitch WX: for a sample of angles, base fractions and depths the
+// 32 lanes' tap addresses are laid out and, per tap, the largest number of
+// distinct addresses that share a bank is counted (1 = conflict-free).
+double bank_cost(const std::vector<double>& xc, const std::vector<double>& yc, int A, int lanes, int nz, int WX) {
+  const int na = std::min(A, 16);
+  double total = 0;
+  int n = 0;
+  int cnt[32];
+  int seen[32][32];
+  for (int s = 0; s < na; ++s) {
+    const int a = (int)((long long)s * A / na);
+    const double a1 = xc[4 * a + 1], a2 = xc[4 * a + 2], a3 = xc[4 * a + 3];
+    const double b1 = yc[4 * a + 1], b2 = yc[4 * a + 2], b3 = yc[4 * a + 3];
+    for (int f = 0; f < 9; ++f) {
+      const double xf = 0.1 + 0.35 * (f % 3), yf = 0.1 + 0.35 * (f / 3);
+      for (int z = 0; z < nz; z += std::max(1, nz / 2)) {
+        int r[32], c[32];
+        for (int l = 0; l < 32; ++l) {
+          const int tx = lanes == 0 ? l : lanes == 1 ? 0 : (l & 7);
+          const int ty = lanes == 0 ? 0 : lanes == 1 ? l : (l >> 3);
+          r[l] = (int)std::floor(yf + b1 * tx + b2 * ty + b3 * z + 64);
+          c[l] = (int)std::floor(xf + a1 * tx + a2 * ty + a3 * z + 64);
+        }
+        for (int t = 0; t < 4; ++t) {
+          std::fill(cnt, cnt + 32, 0);
+          int worst = 0;
+          for (int l = 0; l < 32; ++l) {
+            const int addr = (r[l] + (t >> 1)) * WX + c[l] + (t & 1);
+            const int bank = addr & 31;
+            bool dup = false;
+            for (int q = 0; q < cnt[bank]; ++q) dup = dup || seen[bank][q] == addr;
+            if (!dup) seen[bank][cnt[bank]++] = addr;
+            worst = std::max(worst, cnt[bank]);
+          }
+          total += worst;
+          ++n;
+        }
+      }
+    }
+  }
+  return n ? total / n : 1.0;
+}
+
+}  // namespace
+
 // Window box for a brick of depth nz over all angles of an axis.
 BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
                         int lane) {
@@ -475,9 +531,10 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
     sy += std::fabs(xc[4 * a + 2]) - std::fabs(yc[4 * a + 2]);
     if (yc[4 * a + 3] != 0.0) bz0 = false;
   }
-  p.lane_y = lane < 0 ? sy > sx : lane == 1;  // lane: -1 heuristic, 0 along X, 1 along Y
+  // lane: -1 heuristic (lines along X or Y), 0 lines along X, 1 along Y, 2 patches
+  p.lanes = lane < 0 ? (sy > sx ? 1 : 0) : std::min(lane, 2);
   p.bz0 = bz0;
-  const int BX = p.lane_y ? kConsumerWarps : 32, BY = p.lane_y ? 32 : kConsumerWarps, BZ = nz;
+  const int BX = p.lanes == 1 ? kConsumerWarps : 32, BY = p.lanes == 1 ? 32 : kConsumerWarps, BZ = nz;
   double ex = 0, ey = 0;
   for (int a = 0; a < A; ++a) {
     ex = std::max(ex, std::fabs(xc[4 * a + 1]) * (BX - 1) + std::fabs(xc[4 * a + 2]) * (BY - 1) +
@@ -487,12 +544,28 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
   }
   // taps span [floor(min)-1, floor(max)+1], origin rounded down to the alignment
   const int wx = (int)std::ceil(ex) + 4 + p.align;
-  p.WX = (wx + p.align - 1) / p.align * p.align;
+  const int wx_min = (wx + p.align - 1) / p.align * p.align;
   p.WY = (int)std::ceil(ey) + 4;
+  auto smem_for = [&](int WX) {
+    const size_t stage = (((size_t)WX * p.WY * (half ? 2 : 4)) + 127) & ~(size_t)127;
+    return 128 + ((((size_t)A * sizeof(WinConst)) + 127) & ~(size_t)127) + NST * stage +
+           (((size_t)kConsumerWarps * WX * sizeof(float) + 127) & ~(size_t)127);  // per-warp blended rows
+  };
+  // Row pitch (= box width): the smallest one whose tap loads have the fewest
+  // bank conflicts, among widths that keep 5 CTAs per SM.  A wider box only
+  // loads more of the (zero-filled or unused) detector columns.
+  p.WX = wx_min;
+  double best = 1e30;
+  for (int WX = wx_min; WX <= std::min(256, wx_min + 16 * p.align); WX += p.align) {
+    if (WX > wx_min && smem_for(WX) > (size_t)(228 * 1024 / 5 - 1024)) break;
+    const double c = bank_cost(xc, yc, A, p.lanes, nz, WX);
+    if (c < best - 1e-9) {
+      best = c;
+      p.WX = WX;
+    }
+  }
   p.ok = p.WX <= 256 && p.WY <= 256 && (nz == 4 || nz == 8 || nz == 16);
-  const size_t stage = (((size_t)p.WX * p.WY * (half ? 2 : 4)) + 127) & ~(size_t)127;
-  p.smem = 128 + ((((size_t)A * sizeof(WinConst)) + 127) & ~(size_t)127) + NST * stage +
-           (((size_t)kConsumerWarps * p.WX * sizeof(float) + 127) & ~(size_t)127);  // per-warp blended rows
+  p.smem = smem_for(p.WX);
   if (p.smem > 227 * 1024) p.ok = false;
   return p;
 }
@@ -502,17 +575,17 @@ cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, c
                                    int mode, float step, float* vol_out, float* cbp, void* vol_copy, int copy_kind,
                                    int z0, int z1, int* err, cudaStream_t st) {
   BpArgs P{ax, vol, z0, z1, plan.WX, plan.WY, plan.align, mode, step, vol_out, cbp, vol_copy, copy_kind, err};
-  if (mode == 0) {
-    if (!plan.lane_y && !plan.bz0) return launch_nz<PT, 0, false, false>(map, P, plan, st);
-    if (!plan.lane_y && plan.bz0) return launch_nz<PT, 0, false, true>(map, P, plan, st);
-    if (plan.lane_y && !plan.bz0) return launch_nz<PT, 0, true, false>(map, P, plan, st);
-    return launch_nz<PT, 0, true, true>(map, P, plan, st);
+  if (mode == 0) {  // WBP plans use lines along X or Y
+    if (plan.lanes == 1) return plan.bz0 ? launch_nz<PT, 0, 1, true>(map, P, plan, st)
+                                         : launch_nz<PT, 0, 1, false>(map, P, plan, st);
+    return plan.bz0 ? launch_nz<PT, 0, 0, true>(map, P, plan, st) : launch_nz<PT, 0, 0, false>(map, P, plan, st);
   }
   if constexpr (std::is_same<PT, float>::value) {
-    if (!plan.lane_y && !plan.bz0) return launch_nz<PT, 1, false, false>(map, P, plan, st);
-    if (!plan.lane_y && plan.bz0) return launch_nz<PT, 1, false, true>(map, P, plan, st);
-    if (plan.lane_y && !plan.bz0) return launch_nz<PT, 1, true, false>(map, P, plan, st);
-    return launch_nz<PT, 1, true, true>(map, P, plan, st);
+    if (plan.lanes == 2) return plan.bz0 ? launch_nz<PT, 1, 2, true>(map, P, plan, st)
+                                         : launch_nz<PT, 1, 2, false>(map, P, plan, st);
+    if (plan.lanes == 1) return plan.bz0 ? launch_nz<PT, 1, 1, true>(map, P, plan, st)
+                                         : launch_nz<PT, 1, 1, false>(map, P, plan, st);
+    return plan.bz0 ? launch_nz<PT, 1, 0, true>(map, P, plan, st) : launch_nz<PT, 1, 0, false>(map, P, plan, st);
   }
   return cudaErrorInvalidValue;  // the SIRT update reads the FP32 residual only
 }

@@ -516,6 +516,7 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
                           std::fabs(yc[4 * a + 3]) * (BZ - 1));
   }
   p.WX = ((int)std::ceil(ex) + 4 + 4 + 3) / 4 * 4;
+  if ((p.WX / 4) % 2 == 0) p.WX += 4;  // odd 16-byte units per row: rows start on different banks
   p.WY = (int)std::ceil(ey) + 4;
   const size_t stage = (((size_t)p.WX * p.WY * 4) + 127) & ~(size_t)127;
   // constants for up to A angles (one group) + block-max scratch + 2 stages

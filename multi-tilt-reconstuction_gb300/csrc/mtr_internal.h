@@ -68,7 +68,7 @@ void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, 
 // Window geometry of one axis for the brick shape used by the TMA kernel.
 struct BpPlan {
   bool ok = false;     // window fits the TMA box and shared-memory limits
-  bool lane_y = false; // lanes walk Y (detector x follows volume Y)
+  int lanes = 0;       // warp layout: 0 lines along X, 1 lines along Y, 2 8x4 patches
   bool bz0 = false;    // y map independent of Z for every angle
   int WX = 0, WY = 0;  // window box (elements)
   int align = 4;       // TMA x alignment (elements)
@@ -76,7 +76,8 @@ struct BpPlan {
   size_t smem = 0;     // dynamic shared memory per CTA
 };
 extern const int kBpDepths[3];  // candidate brick depths of the SIRT back-projection
-// lane: -1 picks the lane axis along the larger x-map slope, 0 = X, 1 = Y.
+// lane: -1 picks lines along the larger x-map slope, 0 = lines along X,
+// 1 = lines along Y, 2 = 8x4 patches.
 BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
                         int lane = -1);
 template <typename PT>

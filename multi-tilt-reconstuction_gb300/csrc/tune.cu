@@ -6,12 +6,13 @@
 //    per-angle window work and, in the forward splat, merge more of a
 //    column's taps; shallow bricks give more CTAs on small volumes and use
 //    fewer registers;
-//  * lane axis: lanes along X keep volume accesses coalesced, lanes along the
-//    volume axis that detector x follows keep shared-memory gathers free of
-//    bank conflicts.
-// For each tilt axis the tuner times every candidate (depth 4/8/16 x lane X/Y
-// for the SIRT back-projection, depth 8/16/32 x lane X/Y for the forward
-// splat) with CUDA events on the reconstruction's own buffers, before they
+//  * warp layout: lines along X keep volume accesses coalesced, lines along
+//    the volume axis that detector x follows keep shared-memory gathers free
+//    of bank conflicts, and (back-projection) 8x4 patches keep the taps of an
+//    oblique axis compact in the window.
+// For each tilt axis the tuner times every candidate (depth 4/8/16 x lines
+// along X / lines along Y / patches for the SIRT back-projection, depth
+// 8/16/32 x lines along X / Y for the forward splat) with CUDA events on the reconstruction's own buffers, before they
 // hold data (each candidate launch writes only scratch that the run
 // overwrites), and keeps the fastest.  Results are cached per process by a
 // geometry key and, when MTR_AUTOTUNE_CACHE names a file, persisted there as
@@ -95,7 +96,7 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
   }
   char buf[256];
   // the trailing tag names the timing method, so choices cached by an older one are not reused
-  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t2", a.PX, a.PY,
+  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t4", a.PX, a.PY,
                 a.A, v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
   return buf;
 }
@@ -183,9 +184,9 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
     std::vector<std::pair<int, int>> what;
     std::vector<BpPlan> bps;
     std::vector<CUtensorMap> bmaps;
-    bps.reserve(6);
-    bmaps.reserve(6);
-    for (int lane = 0; lane < 2; ++lane)
+    bps.reserve(9);
+    bmaps.reserve(9);
+    for (int lane = 0; lane < 3; ++lane)
       for (int nz : kBpDepths) {
         BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, false, nz, lane);
         CUtensorMap m;
