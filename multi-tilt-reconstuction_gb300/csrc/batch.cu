@@ -99,13 +99,13 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
       const FwdPlan& fp = a.fplan;
       const int bgx = (v.NX + (bp.lanes == 1 ? 8 : 32) - 1) / (bp.lanes == 1 ? 8 : 32);
       const int bgy = (v.NY + (bp.lanes == 1 ? 32 : 8) - 1) / (bp.lanes == 1 ? 32 : 8);
-      const int fgx = (v.NX + (fp.lane_y ? 8 : 32) - 1) / (fp.lane_y ? 8 : 32);
-      const int fgy = (v.NY + (fp.lane_y ? 32 : 8) - 1) / (fp.lane_y ? 32 : 8);
+      const int fgx = (v.NX + (fp.lanes == 1 ? 8 : 32) - 1) / (fp.lanes == 1 ? 8 : 32);
+      const int fgy = (v.NY + (fp.lanes == 1 ? 32 : 8) - 1) / (fp.lanes == 1 ? 32 : 8);
       // the persistent kernel takes lines along X or Y; patch-tiled axes keep their own launches
       const bool bp_ok = a.tma && !tma_disabled() && bp.lanes != 2 &&
                          (long long)bgx * bgy * ((v.NZ + bp.nz - 1) / bp.nz) <
                              (long long)kOwnWaves * ctx->num_sms * backproject_batch_ctas_per_sm(bp.smem);
-      const bool fwd_ok = a.ftma && !tma_disabled() &&
+      const bool fwd_ok = a.ftma && !tma_disabled() && fp.lanes != 2 &&
                           (long long)fgx * fgy * ((v.NZ + fp.nz - 1) / fp.nz) <
                               (long long)kOwnWaves * ctx->num_sms * forward_ctas_per_sm(ck, fp.smem);
       const int j = (int)maps.size() / 2;
@@ -139,10 +139,10 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
         d.ax = a.dev();
         d.vol = v;
         d.WX = fp.WX; d.WY = fp.WY; d.mass_shift = fp.mass_shift;
-        const int BX = fp.lane_y ? 8 : 32, BY = fp.lane_y ? 32 : 8;
+        const int BX = fp.lanes == 1 ? 8 : 32, BY = fp.lanes == 1 ? 32 : 8;
         d.gx = (v.NX + BX - 1) / BX;
         d.gy = (v.NY + BY - 1) / BY;
-        d.lane_y = fp.lane_y; d.bz0 = fp.bz0; d.nz = fp.nz;
+        d.lane_y = fp.lanes == 1; d.bz0 = fp.bz0; d.nz = fp.nz;
         d.x = ck ? a.xcopy.p : a.x.p;
         d.map = nullptr;
         fwd.push_back(d);

@@ -469,13 +469,12 @@ cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const long long* 
   return cudaGetLastError();
 }
 
-namespace {
-
 // Mean number of shared-memory wavefronts per tap load of one warp for a
 // window row pitch WX: for a sample of angles, base fractions and depths the
 // 32 lanes' tap addresses are laid out and, per tap, the largest number of
 // distinct addresses that share a bank is counted (1 = conflict-free).
-double bank_cost(const std::vector<double>& xc, const std::vector<double>& yc, int A, int lanes, int nz, int WX) {
+double window_bank_cost(const std::vector<double>& xc, const std::vector<double>& yc, int A, int lanes, int nz,
+                        int WX) {
   const int na = std::min(A, 16);
   double total = 0;
   int n = 0;
@@ -514,8 +513,6 @@ double bank_cost(const std::vector<double>& xc, const std::vector<double>& yc, i
   }
   return n ? total / n : 1.0;
 }
-
-}  // namespace
 
 // Window box for a brick of depth nz over all angles of an axis.
 BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
@@ -558,7 +555,7 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
   double best = 1e30;
   for (int WX = wx_min; WX <= std::min(256, wx_min + 16 * p.align); WX += p.align) {
     if (WX > wx_min && smem_for(WX) > (size_t)(228 * 1024 / 5 - 1024)) break;
-    const double c = bank_cost(xc, yc, A, p.lanes, nz, WX);
+    const double c = window_bank_cost(xc, yc, A, p.lanes, nz, WX);
     if (c < best - 1e-9) {
       best = c;
       p.WX = WX;

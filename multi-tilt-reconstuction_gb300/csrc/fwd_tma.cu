@@ -153,11 +153,11 @@ __device__ __forceinline__ void stream_column_row(int* u, const float (&v)[NZ], 
 
 // One brick (bx, by, zb) and angle group g of one axis; `smem` is the CTA's
 // dynamic shared memory.  On return every bulk reduce it issued is complete.
-template <typename VT, bool LANE_Y, bool BZ0, int NZ>
+template <typename VT, int LANES, bool BZ0, int NZ>
 __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs& P, int bx, int by, int zb, int g,
                                           unsigned char* smem) {
-  constexpr int BX = LANE_Y ? kWarps : 32;
-  constexpr int BY = LANE_Y ? 32 : kWarps;
+  constexpr int BX = LANES == 1 ? kWarps : 32;
+  constexpr int BY = LANES == 1 ? 32 : kWarps;
   FwdConst* kc = reinterpret_cast<FwdConst*>(smem);
   const size_t kc_bytes = ((size_t)P.max_angles * sizeof(FwdConst) + 127) & ~(size_t)127;
   const int WX = P.WX, WY = P.WY;
@@ -209,8 +209,9 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
   }
 
   // own voxels, loaded once (coalesced along lanes), and the brick's max |v|
-  const int tx = LANE_Y ? warp : lane;
-  const int ty = LANE_Y ? lane : warp;
+  // LANES: 0 each warp a line along X, 1 a line along Y, 2 an 8x4 patch
+  const int tx = LANES == 0 ? lane : LANES == 1 ? warp : (warp & 3) * 8 + (lane & 7);
+  const int ty = LANES == 0 ? warp : LANES == 1 ? lane : (warp >> 2) * 4 + (lane >> 3);
   const bool active = (X0 + tx < P.vol.Xs + P.vol.NX) && (Y0 + ty < P.vol.Ys + P.vol.NY);
   float v[NZ];
   float vmax = 0.f;
@@ -261,7 +262,7 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
     const FwdConst k = kc[j];
     // Uniform rows: the detector y does not move along the lanes (|slope| * 31
     // below 1e-6 px), so the lanes of a warp share their two rows and weights.
-    if (BZ0 && k.interior && fabsf(k.a3) < 0.999f && fabsf(LANE_Y ? k.b2 : k.b1) < 3e-8f) {
+    if (BZ0 && LANES != 2 && k.interior && fabsf(k.a3) < 0.999f && fabsf(LANES == 1 ? k.b2 : k.b1) < 3e-8f) {
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
       const float yr = __shfl_sync(0xffffffffu, fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf)), 0);
       if (active) {
@@ -374,20 +375,20 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
 }
 
 // One CTA per (brick, angle group) of one axis.
-template <typename VT, bool LANE_Y, bool BZ0, int NZ>
+template <typename VT, int LANES, bool BZ0, int NZ>
 __global__ void __launch_bounds__(kThreads)
 fwd_tma_kernel(const __grid_constant__ CUtensorMap smap, const FwdArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
-  fwd_brick<VT, LANE_Y, BZ0, NZ>(&smap, P, blockIdx.x, blockIdx.y, blockIdx.z / P.groups, blockIdx.z % P.groups,
+  fwd_brick<VT, LANES, BZ0, NZ>(&smap, P, blockIdx.x, blockIdx.y, blockIdx.z / P.groups, blockIdx.z % P.groups,
                                  smem);
 }
 
-template <typename VT, bool LY, bool BZ, int NZ>
+template <typename VT, int LY, bool BZ, int NZ>
 cudaError_t launch_one(const CUtensorMap& map, FwdArgs P, size_t smem, int num_sms, cudaStream_t st) {
   auto kern = fwd_tma_kernel<VT, LY, BZ, NZ>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  const int BX = LY ? kWarps : 32, BY = LY ? 32 : kWarps;
+  const int BX = LY == 1 ? kWarps : 32, BY = LY == 1 ? 32 : kWarps;
   const long long bricks = (long long)((P.vol.NX + BX - 1) / BX) * ((P.vol.NY + BY - 1) / BY) *
                            ((P.z1 - P.z0 + NZ - 1) / NZ);
   // split the angles over several CTAs when there are too few bricks to fill the GPU
@@ -402,12 +403,16 @@ cudaError_t launch_one(const CUtensorMap& map, FwdArgs P, size_t smem, int num_s
 }
 
 // Z-dependent y-maps take the per-tap path and use one depth.
-template <typename VT, bool LY, bool BZ>
+template <typename VT, int LY, bool BZ>
 cudaError_t launch_nz(const CUtensorMap& map, const FwdArgs& P, const FwdPlan& plan, int sms, cudaStream_t st) {
-  if (!BZ || plan.nz == 16) return launch_one<VT, LY, BZ, 16>(map, P, plan.smem, sms, st);
-  if (plan.nz == 8) return launch_one<VT, LY, BZ, 8>(map, P, plan.smem, sms, st);
-  if (plan.nz == 32) return launch_one<VT, LY, BZ, 32>(map, P, plan.smem, sms, st);
-  return cudaErrorInvalidValue;
+  if constexpr (!BZ) {
+    return launch_one<VT, LY, false, 16>(map, P, plan.smem, sms, st);
+  } else {
+    if (plan.nz == 16) return launch_one<VT, LY, true, 16>(map, P, plan.smem, sms, st);
+    if (plan.nz == 8) return launch_one<VT, LY, true, 8>(map, P, plan.smem, sms, st);
+    if (plan.nz == 32) return launch_one<VT, LY, true, 32>(map, P, plan.smem, sms, st);
+    return cudaErrorInvalidValue;
+  }
 }
 
 }  // namespace
@@ -423,8 +428,8 @@ namespace {
 template <typename VT, int NZ>
 __device__ __forceinline__ void fwd_batch_item(const CUtensorMap* map, const FwdArgs& P, const int* b,
                                                unsigned char* smem) {
-  if (b[4] == 3) fwd_brick<VT, true, true, NZ>(map, P, b[0], b[1], b[2], 0, smem);
-  else fwd_brick<VT, false, true, NZ>(map, P, b[0], b[1], b[2], 0, smem);
+  if (b[4] == 3) fwd_brick<VT, 1, true, NZ>(map, P, b[0], b[1], b[2], 0, smem);
+  else fwd_brick<VT, 0, true, NZ>(map, P, b[0], b[1], b[2], 0, smem);
 }
 
 template <typename VT>
@@ -451,8 +456,8 @@ fwd_batch_kernel(const FwdBatchDesc* __restrict__ descs, const long long* __rest
     }
     __syncthreads();
     switch (sB[4]) {
-      case 0: fwd_brick<VT, false, false, 16>(sMap, sP, sB[0], sB[1], sB[2], 0, smem); break;  // z-dependent y-map
-      case 2: fwd_brick<VT, true, false, 16>(sMap, sP, sB[0], sB[1], sB[2], 0, smem); break;
+      case 0: fwd_brick<VT, 0, false, 16>(sMap, sP, sB[0], sB[1], sB[2], 0, smem); break;  // z-dependent y-map
+      case 2: fwd_brick<VT, 1, false, 16>(sMap, sP, sB[0], sB[1], sB[2], 0, smem); break;
       default:
         if (sB[3] == 8) fwd_batch_item<VT, 8>(sMap, sP, sB, smem);
         else if (sB[3] == 32) fwd_batch_item<VT, 32>(sMap, sP, sB, smem);
@@ -504,10 +509,11 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
     sy += std::fabs(xc[4 * a + 2]) - std::fabs(yc[4 * a + 2]);
     if (yc[4 * a + 3] != 0.0) bz0 = false;
   }
-  p.lane_y = lane < 0 ? sy > sx : lane == 1;  // lane: -1 heuristic, 0 along X, 1 along Y
+  // lane: -1 heuristic (lines along X or Y), 0 lines along X, 1 along Y, 2 8x4 patches
+  p.lanes = lane < 0 ? (sy > sx ? 1 : 0) : std::min(lane, 2);
   p.bz0 = bz0;
   p.nz = bz0 ? nz : 16;  // Z-dependent y-maps use one depth
-  const int BX = p.lane_y ? kWarps : 32, BY = p.lane_y ? 32 : kWarps, BZ = p.nz;
+  const int BX = p.lanes == 1 ? kWarps : 32, BY = p.lanes == 1 ? 32 : kWarps, BZ = p.nz;
   double ex = 0, ey = 0;
   for (int a = 0; a < A; ++a) {
     ex = std::max(ex, std::fabs(xc[4 * a + 1]) * (BX - 1) + std::fabs(xc[4 * a + 2]) * (BY - 1) +
@@ -515,14 +521,29 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
     ey = std::max(ey, std::fabs(yc[4 * a + 1]) * (BX - 1) + std::fabs(yc[4 * a + 2]) * (BY - 1) +
                           std::fabs(yc[4 * a + 3]) * (BZ - 1));
   }
-  p.WX = ((int)std::ceil(ex) + 4 + 4 + 3) / 4 * 4;
-  if ((p.WX / 4) % 2 == 0) p.WX += 4;  // odd 16-byte units per row: rows start on different banks
+  const int wx_min = ((int)std::ceil(ex) + 4 + 4 + 3) / 4 * 4;
   p.WY = (int)std::ceil(ey) + 4;
-  const size_t stage = (((size_t)p.WX * p.WY * 4) + 127) & ~(size_t)127;
-  // constants for up to A angles (one group) + block-max scratch + 2 stages
-  // + per-warp row buffers of the uniform-row angles
-  p.smem = ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 128 + 2 * stage +
-           (size_t)kWarps * p.WX * sizeof(int);
+  auto smem_for = [&](int WX) {
+    const size_t stage = (((size_t)WX * p.WY * 4) + 127) & ~(size_t)127;
+    // constants for up to A angles (one group) + block-max scratch + 2 stages
+    // + per-warp row buffers of the uniform-row angles
+    return ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 128 + 2 * stage +
+           (size_t)kWarps * WX * sizeof(int);
+  };
+  // Row pitch (= box width) with the fewest shared-memory bank conflicts of
+  // the warp's splat atomics, searched over a few widths only: a wider window
+  // leaves the interior fast path at more bricks near the detector edge.
+  p.WX = wx_min;
+  double best = 1e30;
+  for (int WX = wx_min; WX <= std::min(std::min(256, pitch), wx_min + 16); WX += 4) {
+    if (WX > wx_min && smem_for(WX) > (size_t)(228 * 1024 / 4 - 1024)) break;
+    const double c = window_bank_cost(xc, yc, A, p.lanes, p.nz, WX);
+    if (c < best - 1e-9) {
+      best = c;
+      p.WX = WX;
+    }
+  }
+  p.smem = smem_for(p.WX);
   // Weight a pixel can receive from one brick: per Z plane at most the number
   // of voxels whose taps reach it, i.e. lattice points in the preimage of a
   // 2x2-pixel square under the in-plane map J (bounding box of J^-1 [-1,1]^2).
@@ -549,10 +570,11 @@ cudaError_t launch_forward_tma(const CUtensorMap& smap, const FwdPlan& plan, con
   int dev = 0, sms = 152;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   FwdArgs P{ax, vol, z0, z1, plan.WX, plan.WY, 1, ax.A, plan.mass_shift, x, err};
-  if (!plan.lane_y && plan.bz0) return launch_nz<VT, false, true>(smap, P, plan, sms, st);
-  if (!plan.lane_y && !plan.bz0) return launch_nz<VT, false, false>(smap, P, plan, sms, st);
-  if (plan.lane_y && plan.bz0) return launch_nz<VT, true, true>(smap, P, plan, sms, st);
-  return launch_nz<VT, true, false>(smap, P, plan, sms, st);
+  if (plan.lanes == 2) return plan.bz0 ? launch_nz<VT, 2, true>(smap, P, plan, sms, st)
+                                       : launch_nz<VT, 2, false>(smap, P, plan, sms, st);
+  if (plan.lanes == 1) return plan.bz0 ? launch_nz<VT, 1, true>(smap, P, plan, sms, st)
+                                       : launch_nz<VT, 1, false>(smap, P, plan, sms, st);
+  return plan.bz0 ? launch_nz<VT, 0, true>(smap, P, plan, sms, st) : launch_nz<VT, 0, false>(smap, P, plan, sms, st);
 }
 
 template cudaError_t launch_forward_tma<float>(const CUtensorMap&, const FwdPlan&, const AxisDev&, const VolDev&,

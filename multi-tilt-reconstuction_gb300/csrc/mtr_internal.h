@@ -76,6 +76,11 @@ struct BpPlan {
   size_t smem = 0;     // dynamic shared memory per CTA
 };
 extern const int kBpDepths[3];  // candidate brick depths of the SIRT back-projection
+// Mean shared-memory wavefronts per tap access of one warp (1 = no bank
+// conflict) for a detector window of row pitch WX, simulated on the host for
+// a sample of the axis' angles; lanes: 0 lines along X, 1 along Y, 2 8x4 patches.
+double window_bank_cost(const std::vector<double>& xc, const std::vector<double>& yc, int A, int lanes, int nz,
+                        int WX);
 // lane: -1 picks lines along the larger x-map slope, 0 = lines along X,
 // 1 = lines along Y, 2 = 8x4 patches.
 BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
@@ -93,7 +98,7 @@ bool encode_tensor_map_3d(CUtensorMap* map, const void* base, bool half, int wid
 // ---- windowed forward splat with TMA reduce (fwd_tma.cu) --------------------
 struct FwdPlan {
   bool ok = false;
-  bool lane_y = false;
+  int lanes = 0;       // warp layout: 0 lines along X, 1 lines along Y, 2 8x4 patches
   bool bz0 = false;
   int WX = 0, WY = 0;
   int mass_shift = 0;  // log2 bound of a pixel's weight from one brick

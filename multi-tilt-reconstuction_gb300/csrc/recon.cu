@@ -614,7 +614,7 @@ mtr_status mtr_recon_describe(const mtr_recon* r, char* buf, int cap) {
                   "\"forward\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\",\"y_has_z\":%s}}",
                   k ? "," : "", k, a.tma ? "true" : "false", a.plan.nz, a.plan.WX, a.plan.WY,
                   a.plan.lanes == 1 ? "y" : a.plan.lanes == 2 ? "patch" : "x", a.ftma ? "true" : "false", a.fplan.nz, a.fplan.WX, a.fplan.WY,
-                  a.fplan.lane_y ? "y" : "x", a.fplan.bz0 ? "false" : "true");
+                  a.fplan.lanes == 1 ? "y" : a.fplan.lanes == 2 ? "patch" : "x", a.fplan.bz0 ? "false" : "true");
     s += t;
   }
   s += "]";

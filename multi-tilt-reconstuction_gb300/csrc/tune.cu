@@ -12,7 +12,7 @@
 //    oblique axis compact in the window.
 // For each tilt axis the tuner times every candidate (depth 4/8/16 x lines
 // along X / lines along Y / patches for the SIRT back-projection, depth
-// 8/16/32 x lines along X / Y for the forward splat) with CUDA events on the reconstruction's own buffers, before they
+// 8/16/32 x the same three layouts for the forward splat) with CUDA events on the reconstruction's own buffers, before they
 // hold data (each candidate launch writes only scratch that the run
 // overwrites), and keeps the fastest.  Results are cached per process by a
 // geometry key and, when MTR_AUTOTUNE_CACHE names a file, persisted there as
@@ -96,7 +96,7 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
   }
   char buf[256];
   // the trailing tag names the timing method, so choices cached by an older one are not reused
-  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t4", a.PX, a.PY,
+  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t5", a.PX, a.PY,
                 a.A, v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
   return buf;
 }
@@ -211,9 +211,9 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
     what.clear();
     std::vector<FwdPlan> fps;
     std::vector<CUtensorMap> fmaps;
-    fps.reserve(6);
-    fmaps.reserve(6);
-    for (int lane = 0; lane < 2; ++lane)
+    fps.reserve(9);
+    fmaps.reserve(9);
+    for (int lane = 0; lane < 3; ++lane)
       for (int nz : kFwdDepths) {
         FwdPlan p = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, nz, lane);
         CUtensorMap m;
