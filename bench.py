@@ -326,6 +326,18 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
                  "rel_l2_vs_fp32": err_plain,
                  "kernels": "bp_gather_kernel + fwd_splat_kernel (global atomics), FP32"}
 
+    # volumes in mapped host memory (MTR_FLAG_HOST_VOLUMES), same precision and inputs
+    host_vol = None
+    if args.config in ("c1", "c2"):
+        ph = mk(prec)
+        ph.flags = mtr.FLAG_HOST_VOLUMES
+        rh = mtr.Recon(ctx, axes, vol, ph, mem_kind=mtr.MEM_DEVICE)
+        rh.run()
+        ms_h = max_over_ranks(time_steps(torch, stream, rh, 1))
+        host_vol = {"ms_per_step": ms_h, "device_bytes": rh.footprint(), "vs_device_resident": ms_h / ms,
+                    "rel_l2_vs_device_resident": rel_l2_np(rh.download(), rec.download())}
+        rh.close()
+
     out_mixed = rec.download()
     out_fp32 = ref32.download()
     # free both device-resident runs before the end-to-end calls allocate their own
@@ -377,7 +389,8 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
            "prof": prof, "launches": launches, "gen_s": gen_s, "meta": meta, "vu": vu,
            "mixed_vs_fp32": float(np.linalg.norm(out_mixed.astype(np.float64) - out_fp32) /
                                   max(np.linalg.norm(out_fp32.astype(np.float64)), 1e-30)),
-           "axes_host": host_axes, "vol": vol, "prec": prec, "err64": err64, "io": io, "plain": plain}
+           "axes_host": host_axes, "vol": vol, "prec": prec, "err64": err64, "io": io, "plain": plain,
+           "host_vol": host_vol}
     rec.close()
     if ref32 is not rec:
         ref32.close()
@@ -742,6 +755,7 @@ def main() -> int:
                      "mixed_over_fp32": r["ms32"] / r["ms"]},
             "plain_fp32": None if r["plain"] is None else {"value": vu / (r["plain"]["ms_per_step"] * 1e-3),
                                                             **r["plain"]},
+            "host_volumes": r["host_vol"],
             "error": {"mixed_vs_fp32_rel_l2": r["mixed_vs_fp32"], **(r["err64"] or {})},
             "e2e": {"value": vu / (r["e2e_ms"] * 1e-3), "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
                     "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"],

@@ -91,6 +91,13 @@ typedef struct mtr_params {
 #define MTR_FLAG_RECORD_NORMS 1
 /* Capture the MACE outer iteration in a CUDA graph and replay it. */
 #define MTR_FLAG_GRAPH 2
+/* Keep the volume-sized arrays (iterates, MACE states, weight sums, forward
+ * copies, consensus: 12-14 B per voxel and axis) in pinned host memory mapped
+ * into the device address space, which the kernels load and store directly
+ * (coherent NVLink-C2C on Grace-based GPUs), and only the projection arrays
+ * in device memory: volumes larger than HBM.  No counterpart in the
+ * reference, which splits Z over MPI ranks (MpiBigData.cpp). */
+#define MTR_FLAG_HOST_VOLUMES 4
 
 /* Fill p with the reference defaults (Options(), ReadAndInitialOptions.h:33-42). */
 void mtr_params_default(mtr_params* p);

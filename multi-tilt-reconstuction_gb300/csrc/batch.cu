@@ -312,7 +312,7 @@ mtr_status mtr_batch_create(mtr_context* ctx, int n, const mtr_instance* inst, c
   b->ctx = ctx;
   b->p = *params;
   mtr_params rp = *params;
-  rp.flags = 0;  // the batch captures its own graph; no norm records
+  rp.flags = params->flags & MTR_FLAG_HOST_VOLUMES;  // the batch captures its own graph; no norm records
   for (int i = 0; i < n; ++i) {
     mtr_recon* r = nullptr;
     mtr_status s = mtr_recon_create(ctx, inst[i].n_axes, inst[i].axes, inst[i].vol, &rp, mem_kind, &r);

@@ -79,16 +79,19 @@ struct DeviceGuard {
   }
 };
 
-// Owning device allocation.
+// Owning allocation addressed by the device: device memory, or (alloc_mapped)
+// pinned host memory mapped into the device address space, which kernels
+// load and store directly (coherently over NVLink-C2C on Grace-based GPUs).
 struct DevBuf {
-  void* p = nullptr;
+  void* p = nullptr;     // device-side address
+  void* host = nullptr;  // host allocation when mapped
   size_t bytes = 0;
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), bytes(o.bytes) { o.p = nullptr; o.bytes = 0; }
+  DevBuf(DevBuf&& o) noexcept : p(o.p), host(o.host), bytes(o.bytes) { o.p = o.host = nullptr; o.bytes = 0; }
   DevBuf& operator=(DevBuf&& o) noexcept {
-    if (this != &o) { reset(); p = o.p; bytes = o.bytes; o.p = nullptr; o.bytes = 0; }
+    if (this != &o) { reset(); p = o.p; host = o.host; bytes = o.bytes; o.p = o.host = nullptr; o.bytes = 0; }
     return *this;
   }
   ~DevBuf() { reset(); }
@@ -99,9 +102,22 @@ struct DevBuf {
     if (e == cudaSuccess) bytes = n; else p = nullptr;
     return e;
   }
+  cudaError_t alloc_mapped(size_t n) {
+    reset();
+    if (n == 0) return cudaSuccess;
+    cudaError_t e = cudaHostAlloc(&host, n, cudaHostAllocMapped | cudaHostAllocPortable);
+    if (e != cudaSuccess) { host = nullptr; return e; }
+    e = cudaHostGetDevicePointer(&p, host, 0);
+    if (e != cudaSuccess) { cudaFreeHost(host); host = p = nullptr; return e; }
+    bytes = n;
+    return cudaSuccess;
+  }
+  // device memory, or mapped host memory when `mapped`
+  cudaError_t alloc_where(size_t n, bool mapped) { return mapped ? alloc_mapped(n) : alloc(n); }
   void reset() {
-    if (p) cudaFree(p);
-    p = nullptr;
+    if (host) cudaFreeHost(host);
+    else if (p) cudaFree(p);
+    p = host = nullptr;
     bytes = 0;
   }
   template <typename T> T* as() const { return static_cast<T*>(p); }

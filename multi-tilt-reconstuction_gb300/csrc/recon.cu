@@ -196,8 +196,8 @@ mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
   }
   // w_k = w_avg; first z_k = 2 w_avg - w_k = w_avg.
   for (auto& a : r->ax) {
-    MTR_CK(ctx, cudaMemcpyAsync(a.w.p, wavg, vbytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    MTR_CK(ctx, cudaMemcpyAsync(a.w.p, wavg, vbytes, cudaMemcpyDefault, ctx->stream));
+    MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDefault, ctx->stream));
     if (ck) {
       ProfScope ps(ctx, MTR_KERNEL_OTHER);
       launch_convert_copy(wavg, a.xcopy.p, ck, nv, ctx->stream);
@@ -322,10 +322,12 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   r->ax.resize(n_axes);
   const bool mx = mixed(params->precision);
   const size_t vb = (size_t)r->nv * 4;
-  MTR_CK(ctx, r->wavg.alloc(vb));
+  // volume arrays in mapped host memory (MTR_FLAG_HOST_VOLUMES) or in HBM
+  const bool hv = (params->flags & MTR_FLAG_HOST_VOLUMES) != 0;
+  MTR_CK(ctx, r->wavg.alloc_where(vb, hv));
   MTR_CK(ctx, r->err.alloc(sizeof(int)));
   MTR_CK(ctx, cudaMemsetAsync(r->err.p, 0, sizeof(int), ctx->stream));
-  r->bytes += vb;
+  r->bytes += hv ? 0 : vb;
   for (int k = 0; k < n_axes; ++k) {
     AxisState& a = r->ax[k];
     a.PX = axes[k].prj.X;
@@ -342,11 +344,11 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     MTR_CK(ctx, a.s.alloc((size_t)a.np * 4));
     MTR_CK(ctx, a.cf.alloc((size_t)a.np * 4));
     MTR_CK(ctx, a.r.alloc((size_t)a.np * 4));
-    MTR_CK(ctx, a.cbp.alloc(vb));
-    MTR_CK(ctx, a.w.alloc(vb));
-    MTR_CK(ctx, a.x.alloc(vb));
-    if (mx) MTR_CK(ctx, a.xcopy.alloc((size_t)r->nv * 2));
-    r->bytes += axis_bytes(a.np, r->nv, params->precision) + 64LL * a.A;
+    MTR_CK(ctx, a.cbp.alloc_where(vb, hv));
+    MTR_CK(ctx, a.w.alloc_where(vb, hv));
+    MTR_CK(ctx, a.x.alloc_where(vb, hv));
+    if (mx) MTR_CK(ctx, a.xcopy.alloc_where((size_t)r->nv * 2, hv));
+    r->bytes += axis_bytes(a.np, hv ? 0 : r->nv, params->precision) + 64LL * a.A;  // device bytes
     MTR_CK(ctx, cudaMemcpyAsync(a.xc.p, axes[k].x_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemcpyAsync(a.yc.p, axes[k].y_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream));
@@ -421,7 +423,7 @@ mtr_status mtr_recon_save(mtr_recon* r, const char* path) {
   bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
   for (int k = -1; ok && k < r->K; ++k) {
     const void* src = k < 0 ? r->wavg.p : r->ax[k].w.p;
-    cudaError_t e = cudaMemcpyAsync(host.data(), src, vb, cudaMemcpyDeviceToHost, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(host.data(), src, vb, cudaMemcpyDefault, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
       std::fclose(f);
@@ -464,7 +466,7 @@ mtr_status mtr_recon_load(mtr_recon* r, const char* path, int* outer_done) {
       return set_error(ctx, MTR_ERR_FORMAT, "truncated checkpoint");
     }
     void* dst = k < 0 ? r->wavg.p : r->ax[k].w.p;
-    cudaError_t e = cudaMemcpyAsync(dst, host.data(), vb, cudaMemcpyHostToDevice, ctx->stream);
+    cudaError_t e = cudaMemcpyAsync(dst, host.data(), vb, cudaMemcpyDefault, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // host buffer is reused
     if (e != cudaSuccess) {
       std::fclose(f);
@@ -523,7 +525,8 @@ mtr_status mtr_recon_download(mtr_recon* r, float* out, int mem_kind) {
   if (!r || !out) return MTR_ERR_INVALID_ARGUMENT;
   mtr_context* ctx = r->ctx;
   DeviceGuard g(ctx->device);
-  const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  // (volume arrays may be mapped host memory: let unified addressing pick the direction)
+  const cudaMemcpyKind kind = cudaMemcpyDefault;
   MTR_CK(ctx, cudaMemcpyAsync(out, r->wavg.p, (size_t)r->nv * 4, kind, ctx->stream));
   if (mem_kind != MTR_MEM_DEVICE) {
     MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
@@ -549,7 +552,8 @@ mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind) {
   if (!r || !out) return MTR_ERR_INVALID_ARGUMENT;
   mtr_context* ctx = r->ctx;
   DeviceGuard g(ctx->device);
-  const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+  // (volume arrays may be mapped host memory: let unified addressing pick the direction)
+  const cudaMemcpyKind kind = cudaMemcpyDefault;
   for (int k = 0; k < r->K; ++k)
     MTR_CK(ctx, cudaMemcpyAsync(out + (size_t)k * r->nv, r->ax[k].w.p, (size_t)r->nv * 4, kind, ctx->stream));
   if (mem_kind != MTR_MEM_DEVICE) MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));

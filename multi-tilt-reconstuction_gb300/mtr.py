@@ -24,7 +24,7 @@ ERR_TIMEOUT, ERR_NOT_READY, ERR_CAPACITY = 8, 9, 10
 
 PREC_FP32, PREC_MIXED_BF16, PREC_MIXED_FP16 = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
-FLAG_RECORD_NORMS, FLAG_GRAPH = 1, 2
+FLAG_RECORD_NORMS, FLAG_GRAPH, FLAG_HOST_VOLUMES = 1, 2, 4
 MAX_AXES = 16
 KERNEL_CLASSES = ["wbp", "forward", "residual", "backproject", "mace", "other"]
 

@@ -99,3 +99,24 @@ def test_convergence_record_and_early_stop(ctx):
         r2.init()
         assert r2.run_until(tol) == expect
         r2.close()
+
+
+@pytest.mark.parametrize("prec", [mtr.PREC_FP32, mtr.PREC_MIXED_BF16])
+def test_host_resident_volumes(ctx, prec):
+    """MTR_FLAG_HOST_VOLUMES: the volume arrays live in mapped host memory
+    that the kernels read and write directly; the result is the device-resident one."""
+    c = cases.get("two_axis")
+    p = mtr.params(iter_times=2, sirt_inner=3, sirt_step=0.5, mace_step=0.8, precision=prec)
+    dev = mtr.Recon(ctx, c.axes, c.vol, p)
+    dev.run()
+    want = dev.download()
+    dev_bytes = dev.footprint()
+    dev.close()
+    ph = mtr.params(iter_times=2, sirt_inner=3, sirt_step=0.5, mace_step=0.8, precision=prec,
+                    flags=mtr.FLAG_HOST_VOLUMES | mtr.FLAG_GRAPH)
+    host = mtr.Recon(ctx, c.axes, c.vol, ph)
+    host.run()
+    got = host.download()
+    assert host.footprint() < dev_bytes  # only the projections are in device memory
+    host.close()
+    assert rel_l2(got, want) < run_to_run_tol(prec)
