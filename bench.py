@@ -54,9 +54,12 @@ CONFIGS = {
 # Per-launch DRAM traffic and instruction count of the dominant kernel, from
 # the ncu captures summarised in profiles/ (one launch of axis 0).
 NCU_PROFILES = {
-    ("c2", "backproject"): {"traffic": 331_134_208 + 161_469_952, "warp_inst": 1_384_493_196,
-                            "duration_ms": 1.272832, "sm_ghz": 2.065, "sms": 152,
+    ("c2", "backproject"): {"traffic": 330_625_024 + 161_167_872, "warp_inst": 1_252_056_806,
+                            "duration_ms": 1.107520, "sm_ghz": 2.072, "sms": 152,
                             "source": "profiles/bp_tma_kernel_3axis_512x512x128.md"},
+    ("c2", "forward"): {"traffic": 128_427_776 + 37_460_736, "warp_inst": 1_515_418_200,
+                        "duration_ms": 1.537952, "sm_ghz": 2.061, "sms": 152,
+                        "source": "profiles/fwd_tma_kernel_3axis_512x512x128.md"},
 }
 
 
