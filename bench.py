@@ -315,7 +315,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     # (global-memory gather and global-atomic splat; MTR_DISABLE_TMA=1 is read
     # at creation and at every launch, so it is set only around this run)
     plain = None
-    if args.config in ("c1", "c2"):
+    if args.extras and args.config in ("c1", "c2"):
         os.environ["MTR_DISABLE_TMA"] = "1"
         try:
             rp = mtr.Recon(ctx, axes, vol, mk(mtr.PREC_FP32), mem_kind=mtr.MEM_DEVICE)
@@ -331,7 +331,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
 
     # volumes in mapped host memory (MTR_FLAG_HOST_VOLUMES), same precision and inputs
     host_vol = None
-    if args.config in ("c1", "c2"):
+    if args.extras and args.config in ("c1", "c2"):
         ph = mk(prec)
         ph.flags = mtr.FLAG_HOST_VOLUMES
         rh = mtr.Recon(ctx, axes, vol, ph, mem_kind=mtr.MEM_DEVICE)
@@ -375,7 +375,7 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
             arr_ms.append(dt * 1e3)
     e2e_ms = max_over_ranks(statistics.mean(arr_ms))
 
-    io = mrc_load_throughput(torch, mtr, ctx, host_axes[0].data)
+    io = mrc_load_throughput(torch, mtr, ctx, host_axes[0].data) if args.extras else None
 
     # error of both paths against the all-FP64 GPU reconstruction of the same inputs
     err64 = None
@@ -682,6 +682,8 @@ def main() -> int:
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64", type=int, default=1, help="1: state both paths' error against the FP64 GPU run")
+    ap.add_argument("--extras", type=int, default=1,
+                    help="1: also time the plain FP32 kernels, host-resident volumes and MRC loading (c1/c2)")
     args = ap.parse_args()
 
     rank = int(os.environ.get("RANK", "0"))
