@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(kThreads)
 mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho, int copy_kind,
             double* __restrict__ dchange) {
   double acc = 0.0, acc2 = 0.0;
+  const double inv_k = 1.0 / (double)K;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float wa = wavg[i];
     float wn[kMaxK];
@@ -95,7 +96,7 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
         sum += (double)wn[k];
       }
     }
-    const float na = (float)(sum / (double)K);
+    const float na = (float)(sum * inv_k);  // FP64 mean; the reciprocal spares an FP64 division
     wavg[i] = na;
     const double d = (double)na - (double)wa;
     acc += d * d;
@@ -144,6 +145,7 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __re
     const long long i0 = (long long)item.y * kBatchChunk;
     const long long i1 = min(D.n, i0 + kBatchChunk);
     const int K = D.K;
+    const double inv_k = 1.0 / (double)K;
     for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
       const float wa = D.wavg[i];
       float wn[kMaxK];
@@ -157,7 +159,7 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __re
           sum += (double)wn[k];
         }
       }
-      const float na = (float)(sum / (double)K);
+      const float na = (float)(sum * inv_k);  // FP64 mean; the reciprocal spares an FP64 division
       D.wavg[i] = na;
 #pragma unroll
       for (int k = 0; k < kMaxK; ++k) {

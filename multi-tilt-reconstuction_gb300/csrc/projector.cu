@@ -13,6 +13,9 @@
 // thread adds float slope * (small offset) to the fraction.  The float part
 // stays below ~100 in magnitude, so the tap position carries ~1e-5 px of
 // error however large the detector is, and the inner loop is pure FP32.
+#include <cstdint>
+#include <type_traits>
+
 #include "mtr_internal.h"
 
 namespace mtr {
@@ -205,21 +208,62 @@ fwd_splat_kernel(AxisDev ax, VolDev vol, const VT* __restrict__ x, float* __rest
 
 // Residual (FunctionOnGPU.cu:228-236): r = b - s/c where c != 0, else b;
 // resets s to zero for the next forward pass; FP64 sum of r^2.
-template <typename BT, typename RT>
+// Four consecutive projection values as floats (16-byte / 8-byte vector loads).
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+__device__ __forceinline__ void ld4(const __half* p, float (&v)[4]) {
+  const uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+  const float2 lo = __half22float2(*reinterpret_cast<const __half2*>(&t.x));
+  const float2 hi = __half22float2(*reinterpret_cast<const __half2*>(&t.y));
+  v[0] = lo.x; v[1] = lo.y; v[2] = hi.x; v[3] = hi.y;
+}
+
+// r = b - s/c for 4 consecutive pixels (c == 0: r = b - s, the reference's
+// residual loop, FunctionOnGPU.cu:228-236), s reset to zero for the next
+// forward pass; returns the sum of the four r^2 (FP32, added into FP64).
+template <typename BT>
+__device__ __forceinline__ float residual4(const BT* b, float* s, const float* c, float* r) {
+  float bv[4];
+  ld4(b, bv);
+  const float4 sv = *reinterpret_cast<const float4*>(s);
+  const float4 cv = __ldg(reinterpret_cast<const float4*>(c));
+  float4 rv;
+  rv.x = bv[0] - (cv.x != 0.f ? sv.x / cv.x : sv.x);
+  rv.y = bv[1] - (cv.y != 0.f ? sv.y / cv.y : sv.y);
+  rv.z = bv[2] - (cv.z != 0.f ? sv.z / cv.z : sv.z);
+  rv.w = bv[3] - (cv.w != 0.f ? sv.w / cv.w : sv.w);
+  *reinterpret_cast<float4*>(r) = rv;
+  *reinterpret_cast<float4*>(s) = make_float4(0.f, 0.f, 0.f, 0.f);
+  return rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+}
+
+// r = b - s/c (c != 0), else b - s (FunctionOnGPU.cu:228-236); also
+// resets s to zero for the next forward pass.  NORM: FP64 sum of r^2 (the
+// FP64 pipe is slow, so it is only accumulated when a norm is recorded).
+// Pixels [0, 4*n4) four per thread and step (the host passes n4 = 0 unless
+// every array is 16-byte aligned), the rest one per thread.
+template <typename BT, bool NORM>
 __global__ void __launch_bounds__(256)
-residual_kernel(long long n, const BT* __restrict__ b, float* __restrict__ s, const float* __restrict__ c,
-                RT* __restrict__ r, double* __restrict__ norm2) {
+residual_kernel(long long n, long long n4, const BT* __restrict__ b, float* __restrict__ s,
+                const float* __restrict__ c, float* __restrict__ r, double* __restrict__ norm2) {
   double acc = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n4; q += stride) {
+    const float sq = residual4(b + 4 * q, s + 4 * q, c + 4 * q, r + 4 * q);
+    if (NORM) acc += (double)sq;
+  }
+  for (long long i = 4 * n4 + blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += stride) {
     float sv = s[i];
     const float cv = c[i];
     if (cv != 0.f) sv = sv / cv;
     const float rv = ld_f(b + i) - sv;
-    r[i] = from_f<RT>(rv);
+    r[i] = rv;
     s[i] = 0.f;
-    acc += (double)rv * (double)rv;
+    if (NORM) acc += (double)(rv * rv);
   }
-  if (norm2) {
+  if (NORM) {
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
     __shared__ double red[8];
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
@@ -241,14 +285,10 @@ residual_batch_kernel(const ResBatchDesc* __restrict__ descs, const long long* _
     const int2 item = work_item(first, n_desc, it);
     const ResBatchDesc& D = descs[item.x];
     const long long i0 = (long long)item.y * kBatchChunk;
-    const long long i1 = min(D.n, i0 + kBatchChunk);
-    for (long long i = i0 + threadIdx.x; i < i1; i += blockDim.x) {
-      float sv = D.s[i];
-      const float cv = D.cf[i];
-      if (cv != 0.f) sv = sv / cv;
-      const float bv = HALF_B ? __half2float(static_cast<const __half*>(D.b)[i]) : static_cast<const float*>(D.b)[i];
-      D.r[i] = bv - sv;
-      D.s[i] = 0.f;
+    const long long i1 = min(D.n, i0 + kBatchChunk);  // both multiples of 8 (row pitch)
+    for (long long i = i0 + 4 * threadIdx.x; i < i1; i += 4 * blockDim.x) {
+      if (HALF_B) residual4(static_cast<const __half*>(D.b) + i, D.s + i, D.cf + i, D.r + i);
+      else residual4(static_cast<const float*>(D.b) + i, D.s + i, D.cf + i, D.r + i);
     }
   }
 }
@@ -282,10 +322,16 @@ void launch_forward(const AxisDev& ax, const VolDev& vol, const VT* x, float* s,
 
 template <typename BT, typename RT>
 void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, double* norm2, cudaStream_t st) {
-  long long blocks = (n + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  long long blocks = (n / 4 + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;  // grid-stride loops cover the rest
   if (blocks < 1) blocks = 1;
-  residual_kernel<BT, RT><<<(unsigned)blocks, 256, 0, st>>>(n, b, s, c, r, norm2);
+  static_assert(std::is_same<RT, float>::value, "the residual is FP32");
+  // vector loads need 16-byte aligned arrays (caller-owned buffers may not be)
+  const bool aligned = ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(s) |
+                         reinterpret_cast<uintptr_t>(c) | reinterpret_cast<uintptr_t>(r)) & 15) == 0;
+  const long long n4 = aligned ? n / 4 : 0;
+  if (norm2) residual_kernel<BT, true><<<(unsigned)blocks, 256, 0, st>>>(n, n4, b, s, c, r, norm2);
+  else residual_kernel<BT, false><<<(unsigned)blocks, 256, 0, st>>>(n, n4, b, s, c, r, nullptr);
 }
 
 void launch_residual_batch(const ResBatchDesc* descs, const long long* first, int n_desc, long long n_items, int half_b,
