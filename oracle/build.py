@@ -1,10 +1,10 @@
-"""Build recipe for the checker side (never part of the product):
+"""Build recipe for the oracle, which is test infrastructure (never part of the product):
 
   oracle/liboracle.so        CPU restatement of the reference's math (oracle.cpp)
   oracle/liborc_refrun.so    harness that runs the reference's own kernels
                              from oracle/_ref/ref_kernels.cubin (ref_runner.cu)
-and, only where the reference sources are present (this is not the case on
-the GPU machine, which uses the prebuilt, git-ignored oracle/_ref/ files):
+and, only where the reference sources are present (elsewhere the prebuilt,
+git-ignored oracle/_ref/ files are used):
   oracle/_ref/ref_kernels.cubin   the reference's FunctionOnGPU.cu, unmodified,
                                   device code for sm_103a
   oracle/_ref/ref_golden          golden-vector generator linked from the

@@ -1,6 +1,6 @@
 // CPU oracle for the multi-axis WBP -> SIRT -> MACE path.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker: the parity tests, the
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
 // smoke check and the CPU-baseline leg of the benchmark call it to produce the
 // expected answer.  It is never linked into the product library and the
 // product never falls back to it.

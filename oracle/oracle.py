@@ -2,7 +2,8 @@
 the reference's own kernels (ref_runner.cu).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and
-by bench.py's CPU-baseline leg, always as the checker, never as the product.
+by bench.py's CPU-baseline leg, always as the oracle results are compared
+with, never as the product.
 
 mode 0 = reference-faithful precision, mode 1 = all FP64 (see oracle.cpp).
 """
