@@ -106,6 +106,11 @@ mtr_status mtr_context_destroy(mtr_context* ctx) {
       cudaEventDestroy(r.b);
     }
     for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
+    for (cudaStream_t s : ctx->side_streams) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+    for (cudaEvent_t e : ctx->sync_events) cudaEventDestroy(e);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   }
   delete ctx;

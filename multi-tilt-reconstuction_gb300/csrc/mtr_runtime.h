@@ -32,6 +32,26 @@ struct mtr_context {
     if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
     return e;
   }
+  // Side streams and fork/join events for work that runs concurrently with
+  // the context stream (one per tilt axis), created on first use.
+  std::vector<cudaStream_t> side_streams;
+  std::vector<cudaEvent_t> sync_events;
+  cudaStream_t side_stream(int k) {
+    while ((int)side_streams.size() <= k) {
+      cudaStream_t s = nullptr;
+      if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return nullptr;
+      side_streams.push_back(s);
+    }
+    return side_streams[(size_t)k];
+  }
+  cudaEvent_t sync_event(int i) {
+    while ((int)sync_events.size() <= i) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return nullptr;
+      sync_events.push_back(e);
+    }
+    return sync_events[(size_t)i];
+  }
 };
 
 namespace mtr {

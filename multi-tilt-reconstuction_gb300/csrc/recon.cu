@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <new>
@@ -218,21 +219,66 @@ mtr_status mtr::recon_enqueue_sirt_bp(mtr_recon* r, int k) { return enqueue_bp(r
 
 namespace {
 
+// The n_inner SIRT iterations of one axis in outer iteration `it`.
+mtr_status enqueue_axis_chain(mtr_recon* r, int k, int it) {
+  const int K = r->K, ni = r->p.sirt_inner, no = r->p.iter_times;
+  double* norms = r->norms.as<double>();
+  AxisState& a = r->ax[k];
+  for (int j = 0; j < ni; ++j) {
+    mtr_status s = enqueue_forward(r, a);
+    if (s != MTR_OK) return s;
+    s = enqueue_residual(r, a, norms && it < no ? norms + ((long long)it * K + k) * ni + j : nullptr);
+    if (s != MTR_OK) return s;
+    s = enqueue_bp(r, a, 1, nullptr);
+    if (s != MTR_OK) return s;
+  }
+  return MTR_OK;
+}
+
+// Axes run their SIRT chains concurrently (each on a side stream, forked
+// from and joined back to the context stream) unless MTR_SERIAL_AXES=1 or
+// per-kernel profiling is on (concurrent kernels would share their event
+// intervals).  The chains touch disjoint buffers until the MACE step.
+bool concurrent_axes(const mtr_recon* r) {
+  const char* e = std::getenv("MTR_SERIAL_AXES");
+  return r->K > 1 && !r->ctx->profiling && !(e && e[0] == '1');
+}
+
+// Restores the context stream when a fork/join section ends early.
+struct StreamRestore {
+  mtr_context* ctx;
+  cudaStream_t main;
+  ~StreamRestore() { ctx->stream = main; }
+};
+
 // MACE outer iterations [first, first + count): n_inner SIRT iterations of
 // every axis, then the MACE step.
 mtr_status enqueue_outer(mtr_recon* r, int first, int count) {
-  const int K = r->K, ni = r->p.sirt_inner, no = r->p.iter_times;
-  double* norms = r->norms.as<double>();
+  mtr_context* ctx = r->ctx;
+  const int K = r->K;
+  const bool par = concurrent_axes(r);
   for (int it = first; it < first + count; ++it) {
-    for (int k = 0; k < K; ++k) {
-      AxisState& a = r->ax[k];
-      for (int j = 0; j < ni; ++j) {
-        mtr_status s = enqueue_forward(r, a);
+    if (!par) {
+      for (int k = 0; k < K; ++k) {
+        mtr_status s = enqueue_axis_chain(r, k, it);
         if (s != MTR_OK) return s;
-        s = enqueue_residual(r, a, norms && it < no ? norms + ((long long)it * K + k) * ni + j : nullptr);
+      }
+    } else {
+      StreamRestore guard{ctx, ctx->stream};
+      cudaEvent_t fork = ctx->sync_event(0);
+      if (!fork) return set_error(ctx, MTR_ERR_CUDA, "event creation");
+      MTR_CK(ctx, cudaEventRecord(fork, guard.main));
+      for (int k = 0; k < K; ++k) {
+        cudaStream_t sk = ctx->side_stream(k);
+        cudaEvent_t join = ctx->sync_event(1 + k);
+        if (!sk || !join) return set_error(ctx, MTR_ERR_CUDA, "side stream creation");
+        MTR_CK(ctx, cudaStreamWaitEvent(sk, fork, 0));
+        ctx->stream = sk;
+        mtr_status s = enqueue_axis_chain(r, k, it);
         if (s != MTR_OK) return s;
-        s = enqueue_bp(r, a, 1, nullptr);
-        if (s != MTR_OK) return s;
+        MTR_CK(ctx, cudaEventRecord(join, sk));
+        ctx->stream = guard.main;
+        MTR_CK(ctx, cudaStreamWaitEvent(guard.main, join, 0));
       }
     }
     mtr_status st = recon_enqueue_mace(r, it);

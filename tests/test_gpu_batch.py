@@ -14,13 +14,21 @@ pytestmark = pytest.mark.gpu
 NAMES = ["mid", "mid_oblique", "two_axis", "four_axis", "single"]
 
 
+# Tiles pinned so that the persistent kernels (warp lines) and the own
+# launches of patch-tiled axes are both exercised; None = tuned.
+@pytest.mark.parametrize("tiles", ["8,16,0,0", "16,16,2,2", None])
 @pytest.mark.parametrize("prec", [mtr.PREC_FP32, mtr.PREC_MIXED_BF16])
-def test_batch_matches_each_instance_alone(ctx, prec):
+def test_batch_matches_each_instance_alone(ctx, monkeypatch, prec, tiles):
+    if tiles:
+        monkeypatch.setenv("MTR_FORCE_DEPTHS", tiles)
     cs = [cases.get(n) for n in NAMES]
     p = mtr.params(iter_times=2, sirt_inner=3, sirt_step=0.5, mace_step=0.8, precision=prec, flags=mtr.FLAG_GRAPH)
     b = mtr.Batch(ctx, [(c.axes, c.vol) for c in cs], p)
     info = b.info()
-    assert info["items"]["forward"] > 0 and info["items"]["backproject"] > 0
+    if tiles == "8,16,0,0":
+        assert info["items"]["forward"] > 0 and info["items"]["backproject"] > 0
+    if tiles == "16,16,2,2":
+        assert info["items"]["own_launch_axes"] > 0
     b.run()
     first = [b.download(i) for i in range(len(cs))]
     b.run()  # graph replay
