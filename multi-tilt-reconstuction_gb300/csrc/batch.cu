@@ -3,21 +3,22 @@
 // Each instance is an mtr_recon (its own buffers, WBP init and MACE state).
 // The SIRT phases of all instances run together: per phase ONE persistent
 // launch whose CTAs (a grid sized to the GPU's resident capacity) take the
-// items of a work list covering every instance and axis:
+// items of a work list covering the small axes of every instance:
 //   forward splat   item = (axis, brick)            fwd_batch_kernel
 //   residual        item = (axis, 64 Ki pixels)     residual_batch_kernel
 //   back-projection item = (axis, brick)            bp_batch_kernel
 //   MACE consensus  item = (instance, 64 Ki voxels) mace_batch_kernel
 // so small instances no longer leave SMs idle.  An axis with enough bricks to
-// fill the GPU for kOwnWaves waves keeps its own single launch instead (its
-// brick arguments then sit in the constant bank, which the persistent kernels
-// have to stage through shared memory).  A work list is a descriptor
-// table in cost order plus the prefix sum of the descriptors' item counts;
-// a CTA finds its descriptor by binary search.  Each axis keeps the brick
-// depth, lane axis and tensor maps it was tuned to.  The whole schedule (WBP
-// init of every instance, n_outer x n_inner SIRT phases, MACE steps) is
-// captured once into a CUDA graph and replayed.  An axis whose detector
-// window fits no TMA box runs its own plain kernels inside the same phase.
+// fill the GPU for kOwnWaves waves, an axis tuned to patch tiles, and an axis
+// whose window fits no TMA box keep their own launches instead (arguments in
+// the constant bank, which the persistent kernels have to stage through
+// shared memory): each such axis' forward -> residual -> back-projection
+// chain runs on a side stream, concurrent with the persistent launches.  A
+// work list is a descriptor table in cost order plus the prefix sum of the
+// descriptors' item counts; a CTA finds its descriptor by binary search.
+// Each axis keeps the brick depth, lane layout and tensor maps it was tuned
+// to.  The whole schedule (WBP init of every instance, n_outer x n_inner SIRT
+// phases, MACE steps) is captured once into a CUDA graph and replayed.
 #include <algorithm>
 #include <memory>
 #include <new>
@@ -77,8 +78,7 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
                                   SirtTables& t) {
   const int ck = copy_kind_of(precision);
   t.copy_kind = ck;
-  t.bp_own.clear();
-  t.fwd_own.clear();
+  t.own.clear();
   t.bp_smem = t.fwd_smem = 0;
   std::vector<CUtensorMap> maps;
   std::vector<BpBatchDesc> bpd;
@@ -91,9 +91,6 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
     const VolDev& v = r->vol;
     for (int k = 0; k < r->K; ++k) {
       AxisState& a = r->ax[k];
-      resd.push_back(ResBatchDesc{a.b.p, a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), a.np});
-      res_count.push_back((a.np + kBatchChunk - 1) / kBatchChunk);
-      res_cost.push_back(1);
       // brick depth, lane axis, windows and tensor maps as tuned for this axis
       const BpPlan& bp = a.plan;
       const FwdPlan& fp = a.fplan;
@@ -101,17 +98,24 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
       const int bgy = (v.NY + (bp.lanes == 1 ? 32 : 8) - 1) / (bp.lanes == 1 ? 32 : 8);
       const int fgx = (v.NX + (fp.lanes == 1 ? 8 : 32) - 1) / (fp.lanes == 1 ? 8 : 32);
       const int fgy = (v.NY + (fp.lanes == 1 ? 32 : 8) - 1) / (fp.lanes == 1 ? 32 : 8);
-      // the persistent kernel takes lines along X or Y; patch-tiled axes keep their own launches
+      // the persistent kernels take lines along X or Y of small axes
       const bool bp_ok = a.tma && !tma_disabled() && bp.lanes != 2 &&
                          (long long)bgx * bgy * ((v.NZ + bp.nz - 1) / bp.nz) <
                              (long long)kOwnWaves * ctx->num_sms * backproject_batch_ctas_per_sm(bp.smem);
       const bool fwd_ok = a.ftma && !tma_disabled() && fp.lanes != 2 &&
                           (long long)fgx * fgy * ((v.NZ + fp.nz - 1) / fp.nz) <
                               (long long)kOwnWaves * ctx->num_sms * forward_ctas_per_sm(ck, fp.smem);
+      if (!bp_ok || !fwd_ok) {  // the whole SIRT chain of this axis runs on its own launches
+        t.own.push_back({r, k});
+        continue;
+      }
+      resd.push_back(ResBatchDesc{a.b.p, a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), a.np});
+      res_count.push_back((a.np + kBatchChunk - 1) / kBatchChunk);
+      res_cost.push_back(1);
       const int j = (int)maps.size() / 2;
       maps.push_back(a.map_r);
       maps.push_back(a.map_s);
-      if (bp_ok) {
+      {
         BpBatchDesc d{};
         d.ax = a.dev();
         d.vol = v;
@@ -131,10 +135,8 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
         bp_count.push_back((long long)d.gx * d.gy * ((v.NZ + d.nz - 1) / d.nz));
         bp_cost.push_back((long long)a.A * d.nz);
         t.bp_smem = std::max(t.bp_smem, bp.smem);
-      } else {
-        t.bp_own.push_back({r, k});
       }
-      if (fwd_ok) {
+      {
         FwdBatchDesc d{};
         d.ax = a.dev();
         d.vol = v;
@@ -150,8 +152,6 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
         fwd_count.push_back((long long)d.gx * d.gy * ((v.NZ + d.nz - 1) / d.nz));
         fwd_cost.push_back((long long)a.A * d.nz);
         t.fwd_smem = std::max(t.fwd_smem, fp.smem);
-      } else {
-        t.fwd_own.push_back({r, k});
       }
     }
   }
@@ -184,6 +184,31 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
 
 mtr_status mtr::enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, int* err) {
   cudaStream_t st = ctx->stream;
+  // Own-launch axes: each axis' forward -> residual -> back-projection chain
+  // on a side stream (round-robin over up to kSides), concurrent with the
+  // persistent launches on the context stream; all joined at the end.
+  // Serial when per-kernel profiling is on.
+  constexpr int kSides = 8;
+  const bool par = !t.own.empty() && !ctx->profiling;
+  const int sides = par ? std::min<int>(kSides, (int)t.own.size()) : 0;
+  if (par) {
+    cudaEvent_t fork = ctx->sync_event(0);
+    if (!fork) return set_error(ctx, MTR_ERR_CUDA, "event creation");
+    MTR_CK(ctx, cudaEventRecord(fork, st));
+    for (int i = 0; i < sides; ++i) {
+      cudaStream_t si = ctx->side_stream(i);
+      if (!si) return set_error(ctx, MTR_ERR_CUDA, "side stream creation");
+      MTR_CK(ctx, cudaStreamWaitEvent(si, fork, 0));
+    }
+  }
+  for (size_t i = 0; i < t.own.size(); ++i) {
+    if (par) ctx->stream = ctx->side_stream((int)(i % (size_t)sides));
+    mtr_status s = recon_enqueue_forward(t.own[i].first, t.own[i].second);
+    if (s == MTR_OK) s = recon_enqueue_residual(t.own[i].first, t.own[i].second);
+    if (s == MTR_OK) s = recon_enqueue_sirt_bp(t.own[i].first, t.own[i].second);
+    ctx->stream = st;
+    if (s != MTR_OK) return s;
+  }
   {
     ProfScope ps(ctx, MTR_KERNEL_FORWARD);
     if (t.n_fwd > 0) {
@@ -200,10 +225,6 @@ mtr_status mtr::enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, in
       if (e != cudaSuccess) return cuda_error(ctx, e, "batched forward");
     }
   }
-  for (auto& f : t.fwd_own) {
-    mtr_status s = recon_enqueue_forward(f.first, f.second);
-    if (s != MTR_OK) return s;
-  }
   if (t.n_res > 0) {
     ProfScope ps(ctx, MTR_KERNEL_RESIDUAL);
     launch_residual_batch(t.res_descs.as<ResBatchDesc>(), t.res_first.as<long long>(), t.n_res_desc, t.n_res,
@@ -219,9 +240,13 @@ mtr_status mtr::enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, in
       if (e != cudaSuccess) return cuda_error(ctx, e, "batched back-projection");
     }
   }
-  for (auto& f : t.bp_own) {
-    mtr_status s = recon_enqueue_sirt_bp(f.first, f.second);
-    if (s != MTR_OK) return s;
+  if (par) {
+    for (int i = 0; i < sides; ++i) {
+      cudaEvent_t join = ctx->sync_event(1 + i);
+      if (!join) return set_error(ctx, MTR_ERR_CUDA, "event creation");
+      MTR_CK(ctx, cudaEventRecord(join, ctx->side_stream(i)));
+      MTR_CK(ctx, cudaStreamWaitEvent(st, join, 0));
+    }
   }
   return MTR_OK;
 }
@@ -383,7 +408,7 @@ mtr_status mtr_batch_info(const mtr_batch* b, long long* voxel_updates_per_run, 
     work_items[1] = b->sirt.n_res;
     work_items[2] = b->sirt.n_bp;
     work_items[3] = b->n_mace;
-    work_items[4] = (long long)(b->sirt.fwd_own.size() + b->sirt.bp_own.size());
+    work_items[4] = (long long)b->sirt.own.size();
   }
   return MTR_OK;
 }

@@ -208,9 +208,10 @@ mtr_status recon_enqueue_mace(mtr_recon* r, int it);
 // Descriptor tables of the persistent SIRT kernels over a set of
 // reconstructions of one precision (batch.cu).  One SIRT iteration of every
 // axis of every member = one forward, one residual and one back-projection
-// launch over the small axes, plus the own launches of axes large enough to
-// fill the GPU alone and of axes whose windows fit no TMA box.  Device
-// buffers only grow, so rebuilding for a changed set reallocates rarely.
+// launch over the small axes, plus the own launch chains of the other axes
+// (large enough to fill the GPU alone, tiled as patches, or with windows that
+// fit no TMA box), which run concurrently on side streams.  Device buffers
+// only grow, so rebuilding for a changed set reallocates rarely.
 struct SirtTables {
   int copy_kind = 0;
   DevBuf maps, bp_descs, fwd_descs, res_descs, bp_first, fwd_first, res_first;
@@ -218,7 +219,7 @@ struct SirtTables {
   long long n_bp = 0, n_fwd = 0, n_res = 0;
   size_t bp_smem = 0, fwd_smem = 0;
   int bp_grid = 0, fwd_grid = 0, ew_grid = 0;
-  std::vector<std::pair<mtr_recon*, int>> bp_own, fwd_own;  // (reconstruction, axis) with their own launches
+  std::vector<std::pair<mtr_recon*, int>> own;  // (reconstruction, axis) with their own launches
 };
 mtr_status build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*>& recs, int precision, SirtTables& t);
 mtr_status enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, int* err);
