@@ -13,10 +13,11 @@
 //
 // Window accumulation is fixed point: shared-memory float atomicAdd is not a
 // single native operation on this part, integer adds are.  Each CTA scales
-// its voxels by a power of two S with S * max|v| < 2^b, b <= 17, so every
-// added value (a tap, or a column's merged run of at most 16 voxels) rounds
-// to an integer below 2^21 (rounded with the 1.5*2^23 trick, no float->int
-// conversion) with an absolute error of at most 2^-(b+1) * max|v|.  The host
+// its voxels by a power of two S with S * max|v| < 2^b, b <= 21 - log2(depth),
+// so every added value (a tap, or a column's merged run of at most depth
+// voxels) rounds to an integer below 2^21 (rounded with the 1.5*2^23 trick,
+// no float->int conversion) with an absolute error of at most
+// 2^-(b+1) * max|v|.  The host
 // bounds the weight one pixel can receive from one brick by 2^mass_shift
 // (lattice points in the preimage of a 2x2-pixel square, times the brick
 // depth) and b <= 30 - mass_shift keeps every window sum below 2^30.  Before
