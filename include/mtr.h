@@ -117,6 +117,12 @@ mtr_status mtr_context_destroy(mtr_context* ctx);
 /* Use an external cudaStream_t (NULL restores the context's own stream). */
 mtr_status mtr_context_set_stream(mtr_context* ctx, void* cuda_stream);
 mtr_status mtr_context_synchronize(mtr_context* ctx);
+/* Reconstruction arrays come from a stream-ordered pool owned by the
+ * context; after mtr_recon_destroy they stay reserved (up to a quarter of
+ * the device memory, or MTR_POOL_KEEP_BYTES) so that the next reconstruction
+ * of similar size allocates nothing.  Returns all reserved, unused pool
+ * memory to the device. */
+mtr_status mtr_context_trim(mtr_context* ctx);
 /* Number of libmtr kernel launches issued by this process so far (graph
  * replays count every kernel node). */
 mtr_status mtr_context_launch_count(const mtr_context* ctx, long long* out);

@@ -111,9 +111,23 @@ mtr_status mtr_context_destroy(mtr_context* ctx) {
       cudaStreamDestroy(s);
     }
     for (cudaEvent_t e : ctx->sync_events) cudaEventDestroy(e);
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    // (a pool with arrays still allocated is released when they are freed)
+    if (ctx->pool) cudaMemPoolDestroy(ctx->pool);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   }
   delete ctx;
+  return MTR_OK;
+}
+
+mtr_status mtr_context_trim(mtr_context* ctx) {
+  if (!ctx) return MTR_ERR_INVALID_ARGUMENT;
+  DeviceGuard g(ctx->device);
+  if (!ctx->pool) return MTR_OK;
+  cudaError_t e = cudaStreamSynchronize(ctx->own_stream);
+  if (e != cudaSuccess) return cuda_error(ctx, e, "cudaStreamSynchronize");
+  e = cudaMemPoolTrimTo(ctx->pool, 0);
+  if (e != cudaSuccess) return cuda_error(ctx, e, "cudaMemPoolTrimTo");
   return MTR_OK;
 }
 

@@ -514,9 +514,11 @@ double window_bank_cost(const std::vector<double>& xc, const std::vector<double>
   return n ? total / n : 1.0;
 }
 
+namespace {
+
 // Window box for a brick of depth nz over all angles of an axis.
-BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
-                        int lane) {
+BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half,
+                                 int nz, int lane) {
   BpPlan p;
   p.align = half ? 8 : 4;
   p.nz = nz;
@@ -565,6 +567,16 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
   p.smem = smem_for(p.WX);
   if (p.smem > 227 * 1024) p.ok = false;
   return p;
+}
+
+PlanMemo<BpPlan> g_bp_plans;
+
+}  // namespace
+
+BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool half, int nz,
+                        int lane) {
+  return g_bp_plans.get(plan_key(xc, yc, A, {half ? 1 : 0, nz, lane}),
+                        [&] { return plan_backproject_uncached(xc, yc, A, half, nz, lane); });
 }
 
 template <typename PT>

@@ -17,12 +17,11 @@
 // so every added value (a tap, or a column's merged run of at most depth
 // voxels) rounds to an integer below 2^21 (rounded with the 1.5*2^23 trick,
 // no float->int conversion) with an absolute error of at most
-// 2^-(b+1) * max|v|.  The host
-// bounds the weight one pixel can receive from one brick by 2^mass_shift
-// (lattice points in the preimage of a 2x2-pixel square, times the brick
-// depth) and b <= 30 - mass_shift keeps every window sum below 2^30.  Before
-// the flush the window is converted back to float and divided by S (exact:
-// S is a power of two).
+// 2^-(b+1) * max|v|.  The host bounds the weight one pixel can receive from
+// one brick by 2^mass_shift (lattice points in the preimage of a 2x2-pixel
+// square, times the brick depth) and b <= 30 - mass_shift keeps every window
+// sum below 2^30.  Before the flush the window is converted back to float and
+// divided by S (exact: S is a power of two).
 //
 // When the y-map has no Z term, a voxel column's y weights are common to the
 // column and its x advances by |a3| < 1 per voxel: the interior path merges
@@ -500,8 +499,10 @@ template cudaError_t launch_forward_batch<__nv_bfloat16>(const FwdBatchDesc*, co
 template cudaError_t launch_forward_batch<__half>(const FwdBatchDesc*, const long long*, int, long long, size_t,
                                                    int, cudaStream_t);
 
-FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch,
-                     int nz, int lane) {
+namespace {
+
+FwdPlan plan_forward_uncached(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY,
+                              int pitch, int nz, int lane) {
   FwdPlan p;
   double sx = 0, sy = 0;
   bool bz0 = true;
@@ -563,6 +564,16 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
          p.smem <= 200 * 1024 && (p.nz == 8 || p.nz == 16 || p.nz == 32);
   (void)PX;
   return p;
+}
+
+PlanMemo<FwdPlan> g_fwd_plans;
+
+}  // namespace
+
+FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& yc, int A, int PX, int PY, int pitch,
+                     int nz, int lane) {
+  return g_fwd_plans.get(plan_key(xc, yc, A, {PX, PY, pitch, nz, lane}),
+                         [&] { return plan_forward_uncached(xc, yc, A, PX, PY, pitch, nz, lane); });
 }
 
 template <typename VT>

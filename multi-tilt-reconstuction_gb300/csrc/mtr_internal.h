@@ -6,7 +6,10 @@
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 #include <cstdint>
+#include <initializer_list>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/mtr.h"
@@ -63,6 +66,41 @@ void launch_forward(const AxisDev& ax, const VolDev& vol, const VT* x, float* s,
 template <typename BT, typename RT>
 void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, double* norm2,
                      cudaStream_t st);
+
+// Exact key of a planner call: its integer arguments and the raw bytes of the
+// 4*A coefficients of both maps.
+inline std::string plan_key(const std::vector<double>& xc, const std::vector<double>& yc, int A,
+                            std::initializer_list<int> args) {
+  std::string k;
+  k.reserve(args.size() * sizeof(int) + 8 * (size_t)A * sizeof(double));
+  for (int v : args) k.append(reinterpret_cast<const char*>(&v), sizeof(int));
+  k.append(reinterpret_cast<const char*>(xc.data()), 4 * (size_t)A * sizeof(double));
+  k.append(reinterpret_cast<const char*>(yc.data()), 4 * (size_t)A * sizeof(double));
+  return k;
+}
+
+// Process-wide memo of planner results.  A plan depends only on the planner's
+// arguments, and planning simulates the warps' shared-memory bank pattern for
+// every candidate row pitch (milliseconds per call), which every
+// reconstruction of an already-seen geometry would otherwise repeat.
+template <typename Plan>
+struct PlanMemo {
+  std::mutex mu;
+  std::unordered_map<std::string, Plan> map;
+  template <typename F>
+  Plan get(std::string key, F&& compute) {
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      auto it = map.find(key);
+      if (it != map.end()) return it->second;
+    }
+    const Plan p = compute();
+    std::lock_guard<std::mutex> lock(mu);
+    if (map.size() >= 4096) map.clear();
+    map.emplace(std::move(key), p);
+    return p;
+  }
+};
 
 // ---- TMA-staged back-projection (bp_tma.cu) -------------------------------
 // Window geometry of one axis for the brick shape used by the TMA kernel.

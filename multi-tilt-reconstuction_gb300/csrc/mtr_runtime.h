@@ -3,6 +3,8 @@
 #pragma once
 
 #include <atomic>
+#include <cstdint>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -51,6 +53,39 @@ struct mtr_context {
       sync_events.push_back(e);
     }
     return sync_events[(size_t)i];
+  }
+  // Stream-ordered pool for the arrays of reconstructions, created on first
+  // use.  Arrays freed by mtr_recon_destroy stay reserved in the pool (up to
+  // its release threshold) and the next reconstruction of similar size takes
+  // them without a cudaMalloc/cudaFree round trip.  nullptr when the device
+  // has no pool support (plain cudaMalloc then).
+  cudaMemPool_t pool = nullptr;
+  bool pool_tried = false;
+  cudaMemPool_t memory_pool() {
+    if (pool_tried) return pool;
+    pool_tried = true;
+    int supported = 0;
+    if (cudaDeviceGetAttribute(&supported, cudaDevAttrMemoryPoolsSupported, device) != cudaSuccess || !supported) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&pool, &props) != cudaSuccess) {
+      cudaGetLastError();
+      pool = nullptr;
+      return nullptr;
+    }
+    // Reserved bytes kept across synchronisations: MTR_POOL_KEEP_BYTES, else
+    // a quarter of the device memory.
+    size_t total = 0, free_b = 0;
+    if (cudaMemGetInfo(&free_b, &total) != cudaSuccess) { cudaGetLastError(); total = 0; }
+    uint64_t keep = (uint64_t)total / 4;
+    if (const char* e = std::getenv("MTR_POOL_KEEP_BYTES")) keep = std::strtoull(e, nullptr, 10);
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    return pool;
   }
 };
 
@@ -109,9 +144,19 @@ struct DevBuf {
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
-  DevBuf(DevBuf&& o) noexcept : p(o.p), host(o.host), bytes(o.bytes) { o.p = o.host = nullptr; o.bytes = 0; }
+  DevBuf(DevBuf&& o) noexcept : p(o.p), host(o.host), bytes(o.bytes), pooled(o.pooled), free_stream(o.free_stream) {
+    o.p = o.host = nullptr;
+    o.bytes = 0;
+    o.pooled = false;
+  }
   DevBuf& operator=(DevBuf&& o) noexcept {
-    if (this != &o) { reset(); p = o.p; host = o.host; bytes = o.bytes; o.p = o.host = nullptr; o.bytes = 0; }
+    if (this != &o) {
+      reset();
+      p = o.p; host = o.host; bytes = o.bytes; pooled = o.pooled; free_stream = o.free_stream;
+      o.p = o.host = nullptr;
+      o.bytes = 0;
+      o.pooled = false;
+    }
     return *this;
   }
   ~DevBuf() { reset(); }
@@ -134,12 +179,41 @@ struct DevBuf {
   }
   // device memory, or mapped host memory when `mapped`
   cudaError_t alloc_where(size_t n, bool mapped) { return mapped ? alloc_mapped(n) : alloc(n); }
+  // Device memory from the context's pool, ordered on the context stream
+  // (usable by work enqueued there after this call, and by any stream once
+  // that stream has been synchronised).  Returned to the pool on the
+  // context's own stream; the owner synchronises the streams that used the
+  // array before releasing it.  Falls back to cudaMalloc without a pool.
+  cudaError_t alloc_pooled(size_t n, mtr_context* ctx) {
+    reset();
+    if (n == 0) return cudaSuccess;
+    cudaMemPool_t pool = ctx->memory_pool();
+    if (!pool) return alloc(n);
+    cudaError_t e = cudaMallocFromPoolAsync(&p, n, pool, ctx->stream);
+    if (e != cudaSuccess) { p = nullptr; return e; }
+    bytes = n;
+    pooled = true;
+    free_stream = ctx->own_stream;
+    if (((uintptr_t)p & 255) != 0) {  // TMA and vector paths want aligned bases
+      reset();
+      return alloc(n);
+    }
+    return cudaSuccess;
+  }
+  // device memory (pooled when `ctx` is given), or mapped host memory
+  cudaError_t alloc_where(size_t n, bool mapped, mtr_context* ctx) {
+    return mapped ? alloc_mapped(n) : alloc_pooled(n, ctx);
+  }
   void reset() {
     if (host) cudaFreeHost(host);
+    else if (p && pooled) cudaFreeAsync(p, free_stream);
     else if (p) cudaFree(p);
     p = host = nullptr;
     bytes = 0;
+    pooled = false;
   }
+  bool pooled = false;
+  cudaStream_t free_stream = nullptr;
   template <typename T> T* as() const { return static_cast<T*>(p); }
 };
 

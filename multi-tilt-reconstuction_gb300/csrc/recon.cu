@@ -359,6 +359,15 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   DeviceGuard g(ctx->device);
   std::unique_ptr<mtr_recon> r(new (std::nothrow) mtr_recon());
   if (!r) return set_error(ctx, MTR_ERR_OUT_OF_MEMORY, "host allocation");
+  // On a failed create, the work already enqueued on the arrays ends before
+  // they go back to the pool (this guard is destroyed before `r`).
+  struct SyncOnFailure {
+    mtr_context* c;
+    const std::unique_ptr<mtr_recon>& r;
+    ~SyncOnFailure() {
+      if (r) cudaStreamSynchronize(c->stream);
+    }
+  } sync_on_failure{ctx, r};
   r->ctx = ctx;
   r->vs = vol;
   r->vol = VolDev{vol.Xstart, vol.Ystart, vol.Zstart, vol.X, vol.Y, vol.Z};
@@ -370,8 +379,8 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   const size_t vb = (size_t)r->nv * 4;
   // volume arrays in mapped host memory (MTR_FLAG_HOST_VOLUMES) or in HBM
   const bool hv = (params->flags & MTR_FLAG_HOST_VOLUMES) != 0;
-  MTR_CK(ctx, r->wavg.alloc_where(vb, hv));
-  MTR_CK(ctx, r->err.alloc(sizeof(int)));
+  MTR_CK(ctx, r->wavg.alloc_where(vb, hv, ctx));
+  MTR_CK(ctx, r->err.alloc_pooled(sizeof(int), ctx));
   MTR_CK(ctx, cudaMemsetAsync(r->err.p, 0, sizeof(int), ctx->stream));
   r->bytes += hv ? 0 : vb;
   for (int k = 0; k < n_axes; ++k) {
@@ -384,16 +393,16 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     a.hxc.assign(axes[k].x_coef, axes[k].x_coef + 4 * a.A);
     a.hyc.assign(axes[k].y_coef, axes[k].y_coef + 4 * a.A);
     const size_t pe = mx ? 2 : 4;
-    MTR_CK(ctx, a.xc.alloc(sizeof(double) * 4 * a.A));
-    MTR_CK(ctx, a.yc.alloc(sizeof(double) * 4 * a.A));
-    MTR_CK(ctx, a.b.alloc((size_t)a.np * pe));
-    MTR_CK(ctx, a.s.alloc((size_t)a.np * 4));
-    MTR_CK(ctx, a.cf.alloc((size_t)a.np * 4));
-    MTR_CK(ctx, a.r.alloc((size_t)a.np * 4));
-    MTR_CK(ctx, a.cbp.alloc_where(vb, hv));
-    MTR_CK(ctx, a.w.alloc_where(vb, hv));
-    MTR_CK(ctx, a.x.alloc_where(vb, hv));
-    if (mx) MTR_CK(ctx, a.xcopy.alloc_where((size_t)r->nv * 2, hv));
+    MTR_CK(ctx, a.xc.alloc_pooled(sizeof(double) * 4 * a.A, ctx));
+    MTR_CK(ctx, a.yc.alloc_pooled(sizeof(double) * 4 * a.A, ctx));
+    MTR_CK(ctx, a.b.alloc_pooled((size_t)a.np * pe, ctx));
+    MTR_CK(ctx, a.s.alloc_pooled((size_t)a.np * 4, ctx));
+    MTR_CK(ctx, a.cf.alloc_pooled((size_t)a.np * 4, ctx));
+    MTR_CK(ctx, a.r.alloc_pooled((size_t)a.np * 4, ctx));
+    MTR_CK(ctx, a.cbp.alloc_where(vb, hv, ctx));
+    MTR_CK(ctx, a.w.alloc_where(vb, hv, ctx));
+    MTR_CK(ctx, a.x.alloc_where(vb, hv, ctx));
+    if (mx) MTR_CK(ctx, a.xcopy.alloc_where((size_t)r->nv * 2, hv, ctx));
     r->bytes += axis_bytes(a.np, hv ? 0 : r->nv, params->precision) + 64LL * a.A;  // device bytes
     MTR_CK(ctx, cudaMemcpyAsync(a.xc.p, axes[k].x_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemcpyAsync(a.yc.p, axes[k].y_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
@@ -414,10 +423,10 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   }
   if (params->flags & MTR_FLAG_RECORD_NORMS) {
     const size_t n = (size_t)std::max(1, params->iter_times) * n_axes * std::max(1, params->sirt_inner);
-    MTR_CK(ctx, r->norms.alloc(sizeof(double) * n));
+    MTR_CK(ctx, r->norms.alloc_pooled(sizeof(double) * n, ctx));
   }
   // convergence record: FP64 sum (w_avg change)^2 and sum w_avg^2 per outer iteration
-  MTR_CK(ctx, r->dchange.alloc(sizeof(double) * 2 * std::max(1, params->iter_times)));
+  MTR_CK(ctx, r->dchange.alloc_pooled(sizeof(double) * 2 * std::max(1, params->iter_times), ctx));
   MTR_CK(ctx, cudaMemsetAsync(r->dchange.p, 0, sizeof(double) * 2 * std::max(1, params->iter_times), ctx->stream));
   s = enqueue_geometry(r.get());
   if (s != MTR_OK) return s;
@@ -675,7 +684,10 @@ mtr_status mtr_recon_describe(const mtr_recon* r, char* buf, int cap) {
 mtr_status mtr_recon_destroy(mtr_recon* r) {
   if (!r) return MTR_OK;
   DeviceGuard g(r->ctx->device);
-  cudaStreamSynchronize(r->ctx->stream);
+  // The arrays return to the context's pool without a further wait, so every
+  // stream that used them must be done: the whole device, as cudaFree would
+  // have waited (the context stream may have been changed since the run).
+  cudaDeviceSynchronize();
   delete r;
   return MTR_OK;
 }

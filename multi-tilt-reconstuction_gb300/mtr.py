@@ -119,6 +119,7 @@ _SIGNATURES = {
     "mtr_context_destroy": (C.c_int, [_P]),
     "mtr_context_set_stream": (C.c_int, [_P, _P]),
     "mtr_context_synchronize": (C.c_int, [_P]),
+    "mtr_context_trim": (C.c_int, [_P]),
     "mtr_context_launch_count": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
     "mtr_context_set_profiling": (C.c_int, [_P, C.c_int]),
     "mtr_context_profile": (C.c_int, [_P, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
@@ -263,6 +264,10 @@ class Context:
 
     def set_stream(self, stream_ptr: int | None) -> None:
         self.check(self.lib.mtr_context_set_stream(self.h, stream_ptr or None), "set_stream")
+
+    def trim(self) -> None:
+        """Return the device memory the context's array pool holds in reserve."""
+        self.check(self.lib.mtr_context_trim(self.h), "mtr_context_trim")
 
     def synchronize(self) -> None:
         self.check(self.lib.mtr_context_synchronize(self.h), "synchronize")

@@ -59,6 +59,7 @@ def test_null_arguments_rejected_without_device():
     assert lib.mtr_context_create(0, None) == mtr.ERR_INVALID_ARGUMENT
     assert lib.mtr_recon_run(None) == mtr.ERR_INVALID_ARGUMENT
     assert lib.mtr_context_destroy(None) == 0
+    assert lib.mtr_context_trim(None) == mtr.ERR_INVALID_ARGUMENT
 
 
 def test_structs_match_c_layout():
