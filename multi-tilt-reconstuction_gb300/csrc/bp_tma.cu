@@ -140,7 +140,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   const int win_elems = P.WX * P.WY;
   const size_t stage_bytes = (((size_t)win_elems * sizeof(PT)) + 127) & ~(size_t)127;
   PT* win0 = reinterpret_cast<PT*>(smem + 128 + kc_bytes);
-  // per-warp blended row (uniform-row angles of the SIRT update)
+  // per-warp blended row (uniform-row angles)
   float* blend = reinterpret_cast<float*>(smem + 128 + kc_bytes + NST * stage_bytes) + (threadIdx.x >> 5) * P.WX;
 
   const int tid = threadIdx.x;
@@ -223,6 +223,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 #pragma unroll
   for (int z = 0; z < NZ; ++z) { s[z] = 0.f; c[z] = 0.f; }
   bool bad = false;
+  int n_inside = 0;  // WBP: angles whose taps of this column all lie on the detector
 
   for (int a = 0; a < A; ++a) {
     const int st = a % NST;
@@ -238,7 +239,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
     // Uniform rows: the detector y does not move along the lanes (|slope| * 31
     // below 1e-6 px), so every lane of the warp reads the same two rows with
     // the same weights; the warp blends them once per angle.
-    const bool uni = BZ0 && MODE == 1 && LANES != 2 && fabsf(LANES == 1 ? k.b2 : k.b1) < 3e-8f;
+    const bool uni = BZ0 && LANES != 2 && fabsf(LANES == 1 ? k.b2 : k.b1) < 3e-8f;
     bool blended = false;
     if (uni) {
       yr = __shfl_sync(0xffffffffu, yr, 0);
@@ -256,7 +257,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
       __syncwarp();
     }
     bool done = !active;
-    if (active && BZ0 && MODE == 1 && fabsf(k.a3) < 0.999f) {
+    if (active && BZ0 && fabsf(k.a3) < 0.999f) {
       // x is affine in z: the column's end voxels bound every tap index, so
       // the window bound is checked once per column instead of per voxel; the
       // stepped tap may run one pixel past the exact last one.
@@ -265,7 +266,15 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
       const int rowi = magic_int(fly) + k.lym;
       const int ixa = magic_int(floorf(xr)) + k.lxm;
       const int ixb = magic_int(floorf(fmaf(k.a3, (float)(NZ - 1), xr))) + k.lxm;
-      if ((unsigned)rowi < lim_y && (unsigned)min(ixa, ixb) < lim_x && (unsigned)(max(ixa, ixb) + 1) < lim_x) {
+      bool inside = (unsigned)rowi < lim_y && (unsigned)min(ixa, ixb) < lim_x && (unsigned)(max(ixa, ixb) + 1) < lim_x;
+      if (MODE == 0) {
+        // WBP also sums the in-detector weights: when both rows and every tap
+        // column of the voxel column lie on the detector, each voxel's four
+        // weights sum to one and the angle adds exactly 1 to its weight sum.
+        const int iy = rowi + k.oy, ix_lo = min(ixa, ixb) + k.ox, ix_hi = max(ixa, ixb) + 1 + k.ox;
+        inside = inside && iy >= 0 && iy + 1 < P.ax.PY && ix_lo >= 0 && ix_hi < P.ax.PX;
+      }
+      if (inside) {
         if (blended) {
           if (k.a3 >= 0.f) bp_column_blended<true, NZ>(s, blend, xr, k.a3, k.lxm);
           else bp_column_blended<false, NZ>(s, blend, xr, k.a3, k.lxm);
@@ -274,6 +283,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
           if (k.a3 >= 0.f) bp_column<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
           else bp_column<false, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
         }
+        if (MODE == 0) ++n_inside;
         done = true;
       }
     }
@@ -334,6 +344,10 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   }
   if (bad) atomicExch(P.err, 5);
   if (!active) return;
+  if (MODE == 0) {
+#pragma unroll
+    for (int z = 0; z < NZ; ++z) c[z] += (float)n_inside;
+  }
 
   const long long sx = P.vol.NX, sxy = (long long)P.vol.NX * P.vol.NY;
   const long long base = (long long)(X0 + tx - P.vol.Xs) + (long long)(Y0 + ty - P.vol.Ys) * sx;
@@ -584,7 +598,9 @@ cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, c
                                    int mode, float step, float* vol_out, float* cbp, void* vol_copy, int copy_kind,
                                    int z0, int z1, int* err, cudaStream_t st) {
   BpArgs P{ax, vol, z0, z1, plan.WX, plan.WY, plan.align, mode, step, vol_out, cbp, vol_copy, copy_kind, err};
-  if (mode == 0) {  // WBP plans use lines along X or Y
+  if (mode == 0) {
+    if (plan.lanes == 2) return plan.bz0 ? launch_nz<PT, 0, 2, true>(map, P, plan, st)
+                                         : launch_nz<PT, 0, 2, false>(map, P, plan, st);
     if (plan.lanes == 1) return plan.bz0 ? launch_nz<PT, 0, 1, true>(map, P, plan, st)
                                          : launch_nz<PT, 0, 1, false>(map, P, plan, st);
     return plan.bz0 ? launch_nz<PT, 0, 0, true>(map, P, plan, st) : launch_nz<PT, 0, 0, false>(map, P, plan, st);

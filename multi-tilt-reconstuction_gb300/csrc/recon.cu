@@ -414,11 +414,13 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     if (!tma_disabled()) {
       // WBP over b; with FP16 projections over their FP32 widening in r (r is
       // free until the first residual), so the WBP gathers FP32 like SIRT.
-      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, false, 8);
-      a.tma_b = a.plan_b.ok && encode_tensor_map_3d(&a.map_b, mx ? a.r.p : a.b.p, false, a.PX, a.pitch, a.PY, a.A,
-                                                    a.plan_b.WX, a.plan_b.WY);
       // SIRT back-projection over the FP32 residual and the forward splat: tuned depths
       tune_axis(ctx, a, r->vol, params->precision, a.w.as<float>(), a.cbp.as<float>(), r->err.as<int>());
+      // The WBP gathers the same windows as the SIRT update: the lane layout
+      // tuned for it (lines or 8x4 patches), at one brick depth.
+      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, false, 8, a.plan.ok ? a.plan.lanes : -1);
+      a.tma_b = a.plan_b.ok && encode_tensor_map_3d(&a.map_b, mx ? a.r.p : a.b.p, false, a.PX, a.pitch, a.PY, a.A,
+                                                    a.plan_b.WX, a.plan_b.WY);
     }
   }
   if (params->flags & MTR_FLAG_RECORD_NORMS) {
