@@ -397,8 +397,9 @@ cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cud
 
 template <typename PT, int MODE, int LANES, bool BZ0>
 cudaError_t launch_nz(const CUtensorMap& map, const BpArgs& P, const BpPlan& plan, cudaStream_t st) {
-  // WBP runs once per reconstruction: one brick depth.  SIRT: the tuned depth.
+  // WBP: depth 16 or 8 (it runs once per reconstruction).  SIRT: the tuned depth.
   if constexpr (MODE == 0) {
+    if (plan.nz == 16) return launch_one<PT, 0, LANES, BZ0, 16>(map, P, plan.smem, st);
     return launch_one<PT, 0, LANES, BZ0, 8>(map, P, plan.smem, st);
   } else {
     if (plan.nz == 8) return launch_one<PT, MODE, LANES, BZ0, 8>(map, P, plan.smem, st);
