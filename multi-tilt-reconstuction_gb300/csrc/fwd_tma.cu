@@ -8,8 +8,9 @@
 // each of its angles it splats the brick into a private detector window in
 // shared memory, then one thread flushes the window into the ray-sum array
 // with a single 3-D tiled cp.reduce.async.bulk.tensor add (the L2 reduces
-// whole sectors).  Two window stages alternate so the flush of one angle
-// overlaps the splat of the next.
+// whole sectors).  Three window stages rotate: the flush of one angle
+// overlaps the splat of the next, and the stage after it is zeroed during the
+// conversion pass, so an angle costs two block barriers.
 //
 // Window accumulation is fixed point: shared-memory float atomicAdd is not a
 // single native operation on this part, integer adds are.  Each CTA scales
@@ -39,6 +40,7 @@ namespace {
 
 constexpr int kWarps = 8;
 constexpr int kThreads = kWarps * 32;
+constexpr int kStages = 3;  // window stages in flight (splat, flush, next)
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kMagicBits = 0x4B400000;
 
@@ -65,6 +67,14 @@ struct FwdArgs {
 };
 
 __device__ __forceinline__ int magic_int(float integral) { return __float_as_int(__fadd_rn(integral, kMagic)); }
+// Zeroes a window stage (16-byte aligned) with all threads of the block.
+__device__ __forceinline__ void zero_window(int* w, int n) {
+  for (int i = threadIdx.x * 4; i < n; i += kThreads * 4) {
+    if (i + 3 < n) *reinterpret_cast<int4*>(w + i) = make_int4(0, 0, 0, 0);
+    else
+      for (int q = i; q < n; ++q) w[q] = 0;
+  }
+}
 __device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 // round(w * v) for |w*v| < 2^22, as an integer, without a conversion instruction
 __device__ __forceinline__ int fixq(float w, float v) { return __float_as_int(fmaf(w, v, kMagic)) - kMagicBits; }
@@ -166,7 +176,7 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
   unsigned char* win0 = smem + kc_bytes + 128;
   float* red = reinterpret_cast<float*>(smem + kc_bytes);  // 32 floats for the block max
   // per-warp row buffers of the uniform-row angles (kept zero between uses)
-  int* urow = reinterpret_cast<int*>(win0 + 2 * stage_bytes) + (threadIdx.x >> 5) * WX;
+  int* urow = reinterpret_cast<int*>(win0 + kStages * stage_bytes) + (threadIdx.x >> 5) * WX;
   for (int i = threadIdx.x & 31; i < WX; i += 32) urow[i] = 0;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -228,12 +238,13 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
   }
   for (int o = 16; o > 0; o >>= 1) vmax = fmaxf(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
   if (lane == 0) red[warp] = vmax;
+  zero_window(reinterpret_cast<int*>(win0), win_elems);  // the first angle's stage
   __syncthreads();
   vmax = red[0];
   for (int w = 1; w < kWarps; ++w) vmax = fmaxf(vmax, red[w]);
   // S = 2^(b-e) with vmax < 2^e, so |v*S| < 2^b.  One emitted value merges at
-  // most NZ = 16 voxels of weight <= 1 each: |emission| < 2^(b+4) <= 2^21, the
-  // range of the magic rounding (b <= 17).  A pixel's window sum stays below
+  // most NZ voxels of weight <= 1 each: |emission| < 2^(b + log2 NZ) <= 2^21,
+  // the range of the magic rounding.  A pixel's window sum stays below
   // 2^(b + mass_shift) <= 2^30 (no int overflow).
   int e2 = 0;
   if (vmax > 0.f && isfinite(vmax)) frexpf(vmax, &e2);
@@ -245,20 +256,15 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
   for (int z = 0; z < NZ; ++z) v[z] *= S;
   if (tid == 0) prefetch_tensormap(smap);
 
+  // Three window stages: angle j splats into stage j % 3 (zeroed while angle
+  // j - 1 was flushed), then converts it while zeroing the stage of angle
+  // j + 1, whose last reader (the bulk reduce of angle j - 2) has finished.
+  // Two block barriers per angle.
   for (int j = 0; j < na; ++j) {
     const int a = a_begin + j;
-    const int st = j & 1;
+    const int st = j % kStages;
     int* wi = reinterpret_cast<int*>(win0 + st * stage_bytes);
     float* wf = reinterpret_cast<float*>(wi);
-    // the bulk reduce that last read this stage (two angles ago) must be done reading
-    if (tid == 0 && j >= 2) bulk_wait_read<1>();
-    __syncthreads();
-    for (int i = tid * 4; i < win_elems; i += kThreads * 4) {
-      if (i + 3 < win_elems) *reinterpret_cast<int4*>(wi + i) = make_int4(0, 0, 0, 0);
-      else
-        for (int q = i; q < win_elems; ++q) wi[q] = 0;
-    }
-    __syncthreads();
     const FwdConst k = kc[j];
     // Uniform rows: the detector y does not move along the lanes (|slope| * 31
     // below 1e-6 px), so the lanes of a warp share their two rows and weights.
@@ -361,9 +367,12 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
         }
       }
     }
+    // the bulk reduce of angle j - 2 (the next stage's last reader) must be done reading
+    if (tid == 0 && j >= 2) bulk_wait_read<1>();
     __syncthreads();
     // fixed point -> float (exact power-of-two scale), in place
     for (int i = tid; i < win_elems; i += kThreads) wf[i] = (float)wi[i] * invS;
+    if (j + 1 < na) zero_window(reinterpret_cast<int*>(win0 + ((j + 1) % kStages) * stage_bytes), win_elems);
     fence_proxy_async_smem();
     __syncthreads();
     if (tid == 0) {
@@ -527,9 +536,9 @@ FwdPlan plan_forward_uncached(const std::vector<double>& xc, const std::vector<d
   p.WY = (int)std::ceil(ey) + 4;
   auto smem_for = [&](int WX) {
     const size_t stage = (((size_t)WX * p.WY * 4) + 127) & ~(size_t)127;
-    // constants for up to A angles (one group) + block-max scratch + 2 stages
-    // + per-warp row buffers of the uniform-row angles
-    return ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 128 + 2 * stage +
+    // constants for up to A angles (one group) + block-max scratch + window
+    // stages + per-warp row buffers of the uniform-row angles
+    return ((((size_t)A * sizeof(FwdConst)) + 127) & ~(size_t)127) + 128 + kStages * stage +
            (size_t)kWarps * WX * sizeof(int);
   };
   // Row pitch (= box width) with the fewest shared-memory bank conflicts of
