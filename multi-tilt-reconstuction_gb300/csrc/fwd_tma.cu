@@ -370,8 +370,16 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
     // the bulk reduce of angle j - 2 (the next stage's last reader) must be done reading
     if (tid == 0 && j >= 2) bulk_wait_read<1>();
     __syncthreads();
-    // fixed point -> float (exact power-of-two scale), in place
-    for (int i = tid; i < win_elems; i += kThreads) wf[i] = (float)wi[i] * invS;
+    // fixed point -> float (exact power-of-two scale), in place, 16 bytes a step
+    for (int i = tid * 4; i < win_elems; i += kThreads * 4) {
+      if (i + 3 < win_elems) {
+        const int4 q = *reinterpret_cast<const int4*>(wi + i);
+        *reinterpret_cast<float4*>(wf + i) =
+            make_float4((float)q.x * invS, (float)q.y * invS, (float)q.z * invS, (float)q.w * invS);
+      } else {
+        for (int e = i; e < win_elems; ++e) wf[e] = (float)wi[e] * invS;
+      }
+    }
     if (j + 1 < na) zero_window(reinterpret_cast<int*>(win0 + ((j + 1) % kStages) * stage_bytes), win_elems);
     fence_proxy_async_smem();
     __syncthreads();
