@@ -378,7 +378,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 // bricks of the same rows at all depths run together, so the detector rows
 // they read stay in L2 instead of being re-read from DRAM once per z layer.
 template <typename PT, int MODE, int LANES, bool BZ0, int NZ>
-__global__ void __launch_bounds__(kThreads, MODE == 1 ? 5 : 4)
+__global__ void __launch_bounds__(kThreads, MODE == 1 ? (NZ >= 32 ? 3 : 5) : 4)
 bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
   bp_brick<PT, MODE, LANES, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
@@ -405,13 +405,14 @@ cudaError_t launch_nz(const CUtensorMap& map, const BpArgs& P, const BpPlan& pla
     if (plan.nz == 8) return launch_one<PT, MODE, LANES, BZ0, 8>(map, P, plan.smem, st);
     if (plan.nz == 4) return launch_one<PT, MODE, LANES, BZ0, 4>(map, P, plan.smem, st);
     if (plan.nz == 16) return launch_one<PT, MODE, LANES, BZ0, 16>(map, P, plan.smem, st);
+    if (plan.nz == 32) return launch_one<PT, MODE, LANES, BZ0, 32>(map, P, plan.smem, st);
     return cudaErrorInvalidValue;
   }
 }
 
 }  // namespace
 
-const int kBpDepths[3] = {4, 8, 16};
+const int kBpDepths[4] = {4, 8, 16, 32};
 
 namespace {
 
@@ -578,7 +579,7 @@ BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vecto
       p.WX = WX;
     }
   }
-  p.ok = p.WX <= 256 && p.WY <= 256 && (nz == 4 || nz == 8 || nz == 16);
+  p.ok = p.WX <= 256 && p.WY <= 256 && (nz == 4 || nz == 8 || nz == 16 || nz == 32);
   p.smem = smem_for(p.WX);
   if (p.smem > 227 * 1024) p.ok = false;
   return p;

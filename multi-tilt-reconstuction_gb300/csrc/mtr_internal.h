@@ -113,7 +113,7 @@ struct BpPlan {
   int nz = 8;          // brick depth (voxels per thread along Z): 4, 8 or 16
   size_t smem = 0;     // dynamic shared memory per CTA
 };
-extern const int kBpDepths[3];  // candidate brick depths of the SIRT back-projection
+extern const int kBpDepths[4];  // candidate brick depths of the SIRT back-projection
 // Mean shared-memory wavefronts per tap access of one warp (1 = no bank
 // conflict) for a detector window of row pitch WX, simulated on the host for
 // a sample of the axis' angles; lanes: 0 lines along X, 1 along Y, 2 8x4 patches.

@@ -417,9 +417,9 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
       // SIRT back-projection over the FP32 residual and the forward splat: tuned depths
       tune_axis(ctx, a, r->vol, params->precision, a.w.as<float>(), a.cbp.as<float>(), r->err.as<int>());
       // The WBP gathers the same windows as the SIRT update: the lane layout
-      // tuned for it (lines or 8x4 patches), at depth 16 where that was the
-      // tuned depth, else 8.
-      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, false, a.plan.ok && a.plan.nz == 16 ? 16 : 8,
+      // tuned for it (lines or 8x4 patches), at depth 16 where the tuned depth
+      // is 16 or more, else 8.
+      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, false, a.plan.ok && a.plan.nz >= 16 ? 16 : 8,
                                   a.plan.ok ? a.plan.lanes : -1);
       a.tma_b = a.plan_b.ok && encode_tensor_map_3d(&a.map_b, mx ? a.r.p : a.b.p, false, a.PX, a.pitch, a.PY, a.A,
                                                     a.plan_b.WX, a.plan_b.WY);

@@ -24,6 +24,7 @@
 #include <cstdlib>
 #include <fstream>
 #include <functional>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -96,7 +97,7 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
   }
   char buf[256];
   // the trailing tag names the timing method, so choices cached by an older one are not reused
-  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t5", a.PX, a.PY,
+  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t6", a.PX, a.PY,
                 a.A, v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
   return buf;
 }
@@ -184,8 +185,9 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
     std::vector<std::pair<int, int>> what;
     std::vector<BpPlan> bps;
     std::vector<CUtensorMap> bmaps;
-    bps.reserve(9);
-    bmaps.reserve(9);
+    // (the candidates keep pointers into these: no reallocation)
+    bps.reserve(3 * std::size(kBpDepths));
+    bmaps.reserve(3 * std::size(kBpDepths));
     for (int lane = 0; lane < 3; ++lane)
       for (int nz : kBpDepths) {
         BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, false, nz, lane);

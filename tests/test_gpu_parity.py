@@ -180,7 +180,7 @@ def test_windowed_and_plain_kernels_agree(ctx, monkeypatch):
 # --- autotuned tile shapes: every depth variant is correct, the cache persists -------
 
 @pytest.mark.parametrize("depths", ["4,8,0,0", "8,16,1,1", "16,32,0,1", "16,8,1,0", "8,32", "16,16,2,0", "4,8,2,1",
-                                    "8,32,0,2", "16,8,2,2"])
+                                    "8,32,0,2", "16,8,2,2", "32,32,0,0", "32,16,2,1", "32,8,1,2"])
 @pytest.mark.parametrize("name", ["mid", "mid_oblique"])
 def test_every_brick_depth_matches_oracle(ctx, monkeypatch, name, depths):
     monkeypatch.setenv("MTR_FORCE_DEPTHS", depths)
