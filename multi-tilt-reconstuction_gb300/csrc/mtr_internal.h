@@ -96,7 +96,7 @@ struct PlanMemo {
     }
     const Plan p = compute();
     std::lock_guard<std::mutex> lock(mu);
-    if (map.size() >= 4096) map.clear();
+    if (map.size() >= 1024) map.clear();  // keys are 64 bytes per angle
     map.emplace(std::move(key), p);
     return p;
   }
