@@ -569,11 +569,21 @@ BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vecto
   // Row pitch (= box width): the smallest one whose tap loads have the fewest
   // bank conflicts, among widths that keep 5 CTAs per SM.  A wider box only
   // loads more of the (zero-filled or unused) detector columns.
+  // A tap's bank is (row * WX + column) mod 32, and two lanes of a warp can
+  // share an address only on the same row (their columns differ by less than
+  // wx_min), so the cost depends on WX mod 32 alone: each residue is
+  // simulated once.
   p.WX = wx_min;
   double best = 1e30;
+  double cost_of[32];
+  bool known[32] = {};
   for (int WX = wx_min; WX <= std::min(256, wx_min + 16 * p.align); WX += p.align) {
     if (WX > wx_min && smem_for(WX) > (size_t)(228 * 1024 / 5 - 1024)) break;
-    const double c = window_bank_cost(xc, yc, A, p.lanes, nz, WX);
+    if (!known[WX & 31]) {
+      cost_of[WX & 31] = window_bank_cost(xc, yc, A, p.lanes, nz, WX);
+      known[WX & 31] = true;
+    }
+    const double c = cost_of[WX & 31];
     if (c < best - 1e-9) {
       best = c;
       p.WX = WX;
