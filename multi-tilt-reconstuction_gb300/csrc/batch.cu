@@ -306,9 +306,35 @@ mtr_status enqueue_batch(mtr_batch* b) {
   mtr_context* ctx = b->ctx;
   cudaStream_t st = ctx->stream;
   MTR_CK(ctx, cudaMemsetAsync(b->err.p, 0, sizeof(int), st));
-  for (mtr_recon* r : b->rec) {
-    mtr_status s = recon_enqueue_init(r);
+  // WBP initialisation of every instance: independent arrays, so the
+  // instances go round-robin onto up to 8 side streams forked from the
+  // context stream and joined back (serial when per-kernel profiling is on).
+  constexpr int kSides = 8;
+  const bool par = b->rec.size() > 1 && !ctx->profiling;
+  const int sides = par ? std::min<int>(kSides, (int)b->rec.size()) : 0;
+  if (par) {
+    cudaEvent_t fork = ctx->sync_event(0);
+    if (!fork) return set_error(ctx, MTR_ERR_CUDA, "event creation");
+    MTR_CK(ctx, cudaEventRecord(fork, st));
+    for (int i = 0; i < sides; ++i) {
+      cudaStream_t si = ctx->side_stream(i);
+      if (!si) return set_error(ctx, MTR_ERR_CUDA, "side stream creation");
+      MTR_CK(ctx, cudaStreamWaitEvent(si, fork, 0));
+    }
+  }
+  for (size_t i = 0; i < b->rec.size(); ++i) {
+    if (par) ctx->stream = ctx->side_stream((int)(i % (size_t)sides));
+    const mtr_status s = recon_enqueue_init(b->rec[i]);
+    ctx->stream = st;
     if (s != MTR_OK) return s;
+  }
+  if (par) {
+    for (int i = 0; i < sides; ++i) {
+      cudaEvent_t join = ctx->sync_event(1 + i);
+      if (!join) return set_error(ctx, MTR_ERR_CUDA, "event creation");
+      MTR_CK(ctx, cudaEventRecord(join, ctx->side_stream(i)));
+      MTR_CK(ctx, cudaStreamWaitEvent(st, join, 0));
+    }
   }
   for (int it = 0; it < b->p.iter_times; ++it) {
     for (int j = 0; j < b->p.sirt_inner; ++j) {
