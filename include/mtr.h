@@ -212,11 +212,18 @@ mtr_status mtr_reconstruct_fp64(mtr_context* ctx, int n_axes, const mtr_axis* ax
 typedef struct mtr_recon mtr_recon;
 
 /* axes[i].prj_data is host memory (mem_kind MTR_MEM_HOST) or device memory
- * (MTR_MEM_DEVICE, float, copied device-to-device). */
+ * (MTR_MEM_DEVICE, float, copied device-to-device).  It may be NULL: that
+ * axis' projections are zero until mtr_recon_upload or mtr_recon_upload_half
+ * supplies them. */
 mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
                             const mtr_params* params, int mem_kind, mtr_recon** out);
 /* Re-upload projection data for axis i (same shape). */
 mtr_status mtr_recon_upload(mtr_recon* r, int axis, const float* prj_data, int mem_kind);
+/* The same from IEEE FP16 projections (AngN*Y*X halves, host or device).  The
+ * mixed-precision paths store projections in FP16 and take them as they are;
+ * the FP32 path widens them on the device.  With mtr_mrc_read_stack_device_half
+ * a stack goes from the file to the reconstruction in half width. */
+mtr_status mtr_recon_upload_half(mtr_recon* r, int axis, const void* prj_f16, int mem_kind);
 /* WBP init + MACE loop on the device (asynchronous on the context stream). */
 mtr_status mtr_recon_run(mtr_recon* r);
 /* The same run in pieces, and checkpoint/resume of the MACE state between
@@ -391,6 +398,9 @@ mtr_status mtr_mrc_read_stack(const char* path, float* out, long long n);
  * copied to the device and widened to float32 there while the next one is
  * read.  Synchronises the context stream before returning. */
 mtr_status mtr_mrc_read_stack_device(mtr_context* ctx, const char* path, float* d_out, long long n);
+/* The same values rounded to IEEE FP16 (round to nearest even) on the device:
+ * d_out holds n halves.  Half the device bytes of the float32 variant. */
+mtr_status mtr_mrc_read_stack_device_half(mtr_context* ctx, const char* path, void* d_out, long long n);
 /* Replaces readCoef (MrcFileIOBaseFunction.cpp:72-134).  Appends x/y
  * coefficients (up to cap each), counts them in *n_x / *n_y, widens *vol by
  * the x->, y->, z-> bound lines and sets vol->X/Y/Z = end - start. */

@@ -207,11 +207,11 @@ mtr_status mtr::check_volume(mtr_context* ctx, const mtr_volume_size& v) {
   return MTR_OK;
 }
 
-mtr_status mtr::check_axis(mtr_context* ctx, const mtr_axis& a) {
+mtr_status mtr::check_axis(mtr_context* ctx, const mtr_axis& a, bool data_required) {
   if (a.prj.X <= 0 || a.prj.Y <= 0 || a.prj.AngN <= 0)
     return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "projection size: X, Y and AngN must be positive");
   if (a.prj.AngN > kMaxAngles) return set_error(ctx, MTR_ERR_UNSUPPORTED, "more angles than supported");
-  if (!a.x_coef || !a.y_coef || !a.prj_data)
+  if (!a.x_coef || !a.y_coef || (data_required && !a.prj_data))
     return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "axis: null coefficient or data pointer");
   for (int i = 0; i < 4 * a.prj.AngN; ++i)
     if (!std::isfinite(a.x_coef[i]) || !std::isfinite(a.y_coef[i]))

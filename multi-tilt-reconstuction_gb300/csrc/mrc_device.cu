@@ -4,9 +4,12 @@
 // the data block is read in large chunks into two pinned host buffers; each
 // chunk's raw bytes are copied to the device and widened to float32 there,
 // while the next chunk is read from the file.  The values are those of
-// mtr_mrc_read_stack (same data offset rule, same per-mode conversion).
+// mtr_mrc_read_stack (same data offset rule, same per-mode conversion); the
+// half-precision variant rounds them to FP16 on the device (round to nearest
+// even), the storage precision of projections in the mixed-precision path.
 #include <cstdint>
 #include <cstdio>
+#include <type_traits>
 #include <sys/types.h>
 
 #include <cuda_fp16.h>
@@ -25,16 +28,24 @@ __device__ __forceinline__ float widen(T v) { return (float)v; }
 template <>
 __device__ __forceinline__ float widen<__half>(__half v) { return __half2float(v); }
 
-template <typename T>
-__global__ void widen_chunk_kernel(const T* __restrict__ src, float* __restrict__ dst, long long n) {
+template <typename O>
+__device__ __forceinline__ O narrow(float v);
+template <>
+__device__ __forceinline__ float narrow<float>(float v) { return v; }
+template <>
+__device__ __forceinline__ __half narrow<__half>(float v) { return __float2half_rn(v); }
+
+template <typename T, typename O>
+__global__ void convert_chunk_kernel(const T* __restrict__ src, O* __restrict__ dst, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    dst[i] = widen(src[i]);
+    dst[i] = narrow<O>(widen(src[i]));
 }
 
-template <typename T>
-void launch_widen_chunk(const void* src, float* dst, long long n, int sms, cudaStream_t st) {
+template <typename T, typename O>
+void launch_convert_chunk(const void* src, O* dst, long long n, int sms, cudaStream_t st) {
   const long long blocks = std::min<long long>((n + 255) / 256, (long long)sms * 16);
-  widen_chunk_kernel<T><<<(unsigned)std::max<long long>(blocks, 1), 256, 0, st>>>(static_cast<const T*>(src), dst, n);
+  convert_chunk_kernel<T, O><<<(unsigned)std::max<long long>(blocks, 1), 256, 0, st>>>(static_cast<const T*>(src),
+                                                                                       dst, n);
 }
 
 int mode_bytes(int mode) {
@@ -64,9 +75,9 @@ struct Staging {
   }
 };
 
-}  // namespace
-
-extern "C" mtr_status mtr_mrc_read_stack_device(mtr_context* ctx, const char* path, float* d_out, long long n) {
+// The data block of `path` as n values of type O (float or __half) at d_out.
+template <typename O>
+mtr_status read_stack_device(mtr_context* ctx, const char* path, O* d_out, long long n) {
   if (!ctx || !path || !d_out || n <= 0) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "invalid argument");
   DeviceGuard g(ctx->device);
   mtr_mrc_header h;
@@ -84,9 +95,12 @@ extern "C" mtr_status mtr_mrc_read_stack_device(mtr_context* ctx, const char* pa
   // the data block is the last n * bytes(mode) bytes of the file (as the host reader)
   if (fseeko(stg.f, (off_t)(size - need), SEEK_SET) != 0) return set_error(ctx, MTR_ERR_IO, "seek");
   const size_t chunk = std::min<size_t>(kChunkBytes, (size_t)need);
+  // float32 data for a float32 result is copied as it is; everything else is
+  // converted on the device from a raw staging chunk
+  const bool direct = h.mode == MTR_MRC_MODE_FLOAT && std::is_same<O, float>::value;
   for (int k = 0; k < 2; ++k) {
     MTR_CK(ctx, cudaHostAlloc(&stg.host[k], chunk, cudaHostAllocDefault));
-    if (h.mode != MTR_MRC_MODE_FLOAT) MTR_CK(ctx, cudaMalloc(&stg.dev[k], chunk));
+    if (!direct) MTR_CK(ctx, cudaMalloc(&stg.dev[k], chunk));
     MTR_CK(ctx, cudaEventCreateWithFlags(&stg.done[k], cudaEventDisableTiming));
   }
   const long long per_chunk = (long long)(chunk / (size_t)nb);
@@ -98,21 +112,34 @@ extern "C" mtr_status mtr_mrc_read_stack_device(mtr_context* ctx, const char* pa
     if (c >= 2) MTR_CK(ctx, cudaEventSynchronize(stg.done[k]));
     if (std::fread(stg.host[k], (size_t)nb, (size_t)m, stg.f) != (size_t)m)
       return set_error(ctx, MTR_ERR_IO, std::string("short read from ") + path);
-    if (h.mode == MTR_MRC_MODE_FLOAT) {
+    if (direct) {
       MTR_CK(ctx, cudaMemcpyAsync(d_out + done, stg.host[k], (size_t)m * 4, cudaMemcpyHostToDevice, ctx->stream));
     } else {
       MTR_CK(ctx, cudaMemcpyAsync(stg.dev[k], stg.host[k], (size_t)m * nb, cudaMemcpyHostToDevice, ctx->stream));
+      O* dst = d_out + done;
+      const int sms = ctx->num_sms;
       switch (h.mode) {
-        case MTR_MRC_MODE_BYTE: launch_widen_chunk<uint8_t>(stg.dev[k], d_out + done, m, ctx->num_sms, ctx->stream); break;
-        case MTR_MRC_MODE_SHORT: launch_widen_chunk<int16_t>(stg.dev[k], d_out + done, m, ctx->num_sms, ctx->stream); break;
-        case MTR_MRC_MODE_USHORT: launch_widen_chunk<uint16_t>(stg.dev[k], d_out + done, m, ctx->num_sms, ctx->stream); break;
-        default: launch_widen_chunk<__half>(stg.dev[k], d_out + done, m, ctx->num_sms, ctx->stream); break;
+        case MTR_MRC_MODE_BYTE: launch_convert_chunk<uint8_t, O>(stg.dev[k], dst, m, sms, ctx->stream); break;
+        case MTR_MRC_MODE_SHORT: launch_convert_chunk<int16_t, O>(stg.dev[k], dst, m, sms, ctx->stream); break;
+        case MTR_MRC_MODE_USHORT: launch_convert_chunk<uint16_t, O>(stg.dev[k], dst, m, sms, ctx->stream); break;
+        case MTR_MRC_MODE_FLOAT: launch_convert_chunk<float, O>(stg.dev[k], dst, m, sms, ctx->stream); break;
+        default: launch_convert_chunk<__half, O>(stg.dev[k], dst, m, sms, ctx->stream); break;
       }
-      MTR_CK_LAUNCH(ctx, "widen MRC chunk");
+      MTR_CK_LAUNCH(ctx, "convert MRC chunk");
     }
     MTR_CK(ctx, cudaEventRecord(stg.done[k], ctx->stream));
     done += m;
   }
   MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return MTR_OK;
+}
+
+}  // namespace
+
+extern "C" mtr_status mtr_mrc_read_stack_device(mtr_context* ctx, const char* path, float* d_out, long long n) {
+  return read_stack_device<float>(ctx, path, d_out, n);
+}
+
+extern "C" mtr_status mtr_mrc_read_stack_device_half(mtr_context* ctx, const char* path, void* d_out, long long n) {
+  return read_stack_device<__half>(ctx, path, static_cast<__half*>(d_out), n);
 }

@@ -119,7 +119,8 @@ extern std::atomic<long long> g_launches;
 mtr_status set_error(mtr_context* ctx, mtr_status s, const std::string& msg);
 mtr_status cuda_error(mtr_context* ctx, cudaError_t e, const char* what);
 mtr_status check_volume(mtr_context* ctx, const mtr_volume_size& v);
-mtr_status check_axis(mtr_context* ctx, const mtr_axis& a);
+// data_required false: prj_data may be null (projections uploaded later).
+mtr_status check_axis(mtr_context* ctx, const mtr_axis& a, bool data_required = true);
 
 // Makes a device current for a scope and restores the previous one.
 struct DeviceGuard {

@@ -77,6 +77,24 @@ mtr_status upload_projections(mtr_recon* r, int k, const float* data, int mem_ki
   return MTR_OK;
 }
 
+// FP16 projections [A][PY][PX] (caller layout).  Mixed precision stores
+// projections as FP16: they go straight into b.  The FP32 path stages them in
+// the forward accumulator and widens them into b.
+mtr_status upload_projections_half(mtr_recon* r, int k, const void* data, int mem_kind) {
+  mtr_context* ctx = r->ctx;
+  AxisState& a = r->ax[k];
+  const cudaMemcpyKind kind = mem_kind == MTR_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  __half* dst = mixed(r->p.precision) ? a.b.as<__half>() : a.s.as<__half>();
+  if (a.pitch != a.PX) MTR_CK(ctx, cudaMemsetAsync(dst, 0, (size_t)a.np * sizeof(__half), ctx->stream));
+  MTR_CK(ctx, cudaMemcpy2DAsync(dst, (size_t)a.pitch * sizeof(__half), data, (size_t)a.PX * sizeof(__half),
+                                (size_t)a.PX * sizeof(__half), (size_t)a.PY * a.A, kind, ctx->stream));
+  if (mixed(r->p.precision)) return MTR_OK;
+  launch_widen(a.s.as<__half>(), a.b.as<float>(), a.np, ctx->stream);
+  MTR_CK_LAUNCH(ctx, "widen projections");
+  MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream));
+  return MTR_OK;
+}
+
 // Geometry-only arrays: forward row sums cf = A 1.  (cbp is produced by WBP.)
 mtr_status enqueue_geometry(mtr_recon* r) {
   mtr_context* ctx = r->ctx;
@@ -353,7 +371,7 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   s = check_params(ctx, *params);
   if (s != MTR_OK) return s;
   for (int k = 0; k < n_axes; ++k) {
-    s = check_axis(ctx, axes[k]);
+    s = check_axis(ctx, axes[k], false);  // null data: uploaded later
     if (s != MTR_OK) return s;
   }
   DeviceGuard g(ctx->device);
@@ -408,8 +426,12 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     MTR_CK(ctx, cudaMemcpyAsync(a.yc.p, axes[k].y_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream));
     MTR_CK(ctx, cudaMemsetAsync(a.r.p, 0, (size_t)a.np * 4, ctx->stream));
-    s = upload_projections(r.get(), k, axes[k].prj_data, mem_kind);
-    if (s != MTR_OK) return s;
+    if (axes[k].prj_data) {
+      s = upload_projections(r.get(), k, axes[k].prj_data, mem_kind);
+      if (s != MTR_OK) return s;
+    } else {  // zero until mtr_recon_upload / mtr_recon_upload_half
+      MTR_CK(ctx, cudaMemsetAsync(a.b.p, 0, (size_t)a.np * pe, ctx->stream));
+    }
     // TMA kernels where the window geometry fits (else the plain kernels run).
     if (!tma_disabled()) {
       // WBP over b; with FP16 projections over their FP32 widening in r (r is
@@ -445,6 +467,14 @@ mtr_status mtr_recon_upload(mtr_recon* r, int axis, const float* prj_data, int m
   if (!r || !prj_data || axis < 0 || axis >= r->K) return MTR_ERR_INVALID_ARGUMENT;
   DeviceGuard g(r->ctx->device);
   return upload_projections(r, axis, prj_data, mem_kind);
+}
+
+mtr_status mtr_recon_upload_half(mtr_recon* r, int axis, const void* prj_f16, int mem_kind) {
+  if (!r || !prj_f16 || axis < 0 || axis >= r->K) return MTR_ERR_INVALID_ARGUMENT;
+  if (mem_kind != MTR_MEM_HOST && mem_kind != MTR_MEM_DEVICE)
+    return set_error(r->ctx, MTR_ERR_INVALID_ARGUMENT, "unknown memory kind");
+  DeviceGuard g(r->ctx->device);
+  return upload_projections_half(r, axis, prj_f16, mem_kind);
 }
 
 mtr_status mtr_recon_init(mtr_recon* r) {

@@ -135,6 +135,7 @@ _SIGNATURES = {
     "mtr_recon_create": (C.c_int, [_P, C.c_int, C.POINTER(AxisC), VolumeSize, C.POINTER(Params), C.c_int,
                                    C.POINTER(_P)]),
     "mtr_recon_upload": (C.c_int, [_P, C.c_int, _P, C.c_int]),
+    "mtr_recon_upload_half": (C.c_int, [_P, C.c_int, _P, C.c_int]),
     "mtr_recon_run": (C.c_int, [_P]),
     "mtr_recon_init": (C.c_int, [_P]),
     "mtr_recon_run_outer": (C.c_int, [_P, C.c_int, C.c_int]),
@@ -168,6 +169,7 @@ _SIGNATURES = {
     "mtr_mrc_read_header": (C.c_int, [C.c_char_p, C.POINTER(MrcHeader)]),
     "mtr_mrc_read_stack": (C.c_int, [C.c_char_p, _P, C.c_longlong]),
     "mtr_mrc_read_stack_device": (C.c_int, [_P, C.c_char_p, _P, C.c_longlong]),
+    "mtr_mrc_read_stack_device_half": (C.c_int, [_P, C.c_char_p, _P, C.c_longlong]),
     "mtr_txbr_read": (C.c_int, [C.c_char_p, _P, _P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                 C.POINTER(VolumeSize)]),
     "mtr_volume_size_empty": (None, [C.POINTER(VolumeSize)]),
@@ -214,7 +216,9 @@ def _ptr(a) -> int:
 
 @dataclass
 class AxisData:
-    """One tilt axis: data [AngN, Y, X] float32 (numpy or CUDA tensor), coefficient arrays [AngN*4]."""
+    """One tilt axis: data [AngN, Y, X] float32 (numpy or CUDA tensor), coefficient arrays [AngN*4].
+    `data` may instead be the shape tuple (AngN, Y, X) of an axis whose
+    projections are uploaded after mtr_recon_create."""
     x_coef: np.ndarray
     y_coef: np.ndarray
     data: object
@@ -225,12 +229,13 @@ class AxisData:
 
     @property
     def prj(self) -> ProjectionSize:
-        a, y, x = tuple(self.data.shape)
+        a, y, x = tuple(self.data) if isinstance(self.data, tuple) else tuple(self.data.shape)
         return ProjectionSize(x, y, a)
 
     def c_struct(self) -> AxisC:
         dp = C.POINTER(C.c_double)
-        return AxisC(self.prj, self.x_coef.ctypes.data_as(dp), self.y_coef.ctypes.data_as(dp), _ptr(self.data))
+        ptr = None if isinstance(self.data, tuple) else _ptr(self.data)
+        return AxisC(self.prj, self.x_coef.ctypes.data_as(dp), self.y_coef.ctypes.data_as(dp), ptr)
 
 
 def params(iter_times=5, sirt_inner=10, sirt_step=0.5, mace_step=0.7, precision=PREC_FP32, flags=0) -> Params:
@@ -354,6 +359,10 @@ class Recon:
 
     def upload(self, k: int, data, mem_kind=MEM_HOST) -> None:
         self.ctx.check(self.ctx.lib.mtr_recon_upload(self.h, k, _ptr(data), mem_kind), "mtr_recon_upload")
+
+    def upload_half(self, k: int, data, mem_kind=MEM_HOST) -> None:
+        """Projections of axis k as IEEE FP16 (numpy float16 or a CUDA half tensor)."""
+        self.ctx.check(self.ctx.lib.mtr_recon_upload_half(self.h, k, _ptr(data), mem_kind), "mtr_recon_upload_half")
 
     def run(self) -> None:
         self.ctx.check(self.ctx.lib.mtr_recon_run(self.h), "mtr_recon_run")
@@ -555,6 +564,12 @@ def read_mrc_stack_device(ctx: "Context", path: str, out) -> None:
     """Read an MRC stack's data into a CUDA float32 tensor `out` (numel = nx*ny*nz)."""
     ctx.check(ctx.lib.mtr_mrc_read_stack_device(ctx.h, str(path).encode(), _ptr(out), out.numel()),
               "mtr_mrc_read_stack_device")
+
+
+def read_mrc_stack_device_half(ctx: "Context", path: str, out) -> None:
+    """Read an MRC stack's data into a CUDA float16 tensor `out`, rounded on the device."""
+    ctx.check(ctx.lib.mtr_mrc_read_stack_device_half(ctx.h, str(path).encode(), _ptr(out), out.numel()),
+              "mtr_mrc_read_stack_device_half")
 
 
 def read_txbr(path: str, cap: int, vol: VolumeSize | None = None):

@@ -60,6 +60,8 @@ def test_null_arguments_rejected_without_device():
     assert lib.mtr_recon_run(None) == mtr.ERR_INVALID_ARGUMENT
     assert lib.mtr_context_destroy(None) == 0
     assert lib.mtr_context_trim(None) == mtr.ERR_INVALID_ARGUMENT
+    assert lib.mtr_recon_upload_half(None, 0, None, 0) == mtr.ERR_INVALID_ARGUMENT
+    assert lib.mtr_mrc_read_stack_device_half(None, b"x.mrc", None, 1) == mtr.ERR_INVALID_ARGUMENT
 
 
 def test_structs_match_c_layout():

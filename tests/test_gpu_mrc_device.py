@@ -1,6 +1,8 @@
 """MRC stacks read straight into device memory (mtr_mrc_read_stack_device)
 give exactly the values of the host reader, for every supported mode and
-across chunk boundaries."""
+across chunk boundaries; the half-precision reader gives those values
+rounded to FP16, and FP16 projections uploaded into a reconstruction
+(mtr_recon_upload_half) give the reconstruction of the same rounded data."""
 import numpy as np
 import pytest
 
@@ -56,3 +58,39 @@ def test_device_read_errors(ctx, tmp_path):
     with pytest.raises(mtr.MtrError) as e:
         mtr.read_mrc_stack_device(ctx, path, big)  # more values asked than the file holds
     assert e.value.status == mtr.ERR_FORMAT
+
+
+@pytest.mark.parametrize("mode", [1, 2, 12])
+def test_half_read_equals_host_read_rounded(ctx, tmp_path, mode):
+    import torch
+
+    rng = np.random.default_rng(10 + mode)
+    lo, hi = {1: (-30000, 30000), 2: (-1e3, 1e3), 12: (-100, 100)}[mode]
+    data = rng.uniform(lo, hi, (5, 31, 47)).astype(np.float32)
+    path = tmp_path / f"h{mode}.mrc"
+    mtr.write_mrc_stack(path, data, mode)
+    host = mtr.read_mrc_stack(path)
+    dev = torch.empty(host.size, dtype=torch.float16, device="cuda")
+    mtr.read_mrc_stack_device_half(ctx, path, dev)
+    got = dev.cpu().numpy().reshape(host.shape).view(np.uint16)
+    np.testing.assert_array_equal(got, host.astype(np.float16).view(np.uint16))
+
+
+@pytest.mark.parametrize("prec", [mtr.PREC_MIXED_BF16, mtr.PREC_FP32])
+def test_half_upload_reconstructs_the_rounded_data(ctx, prec):
+    import cases
+    from conftest import rel_l2, run_to_run_tol
+
+    c = cases.get("two_axis")
+    p = mtr.params(iter_times=2, sirt_inner=3, sirt_step=0.5, mace_step=0.8, precision=prec)
+    halves = [np.ascontiguousarray(np.asarray(a.data, dtype=np.float32).astype(np.float16)) for a in c.axes]
+    rounded = [mtr.AxisData(a.x_coef, a.y_coef, h.astype(np.float32)) for a, h in zip(c.axes, halves)]
+    want = ctx.reconstruct(rounded, c.vol, p)
+    deferred = [mtr.AxisData(a.x_coef, a.y_coef, tuple(np.shape(a.data))) for a in c.axes]
+    r = mtr.Recon(ctx, deferred, c.vol, p)
+    for k, h in enumerate(halves):
+        r.upload_half(k, h)
+    r.run()
+    got = r.download()
+    r.close()
+    assert rel_l2(got, want) < run_to_run_tol(prec)
