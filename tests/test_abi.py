@@ -70,6 +70,19 @@ def test_structs_match_c_layout():
     assert ctypes.sizeof(mtr.ProjectionSize) == 12
 
 
+def test_shape_only_axis_passes_null_data():
+    """An axis given as a shape has no data pointer: mtr_recon_create then
+    leaves its projections zero until an upload."""
+    import numpy as np
+
+    coef = np.zeros(4 * 3)
+    a = mtr.AxisData(coef, coef, (3, 5, 7)).c_struct()
+    assert (a.prj.X, a.prj.Y, a.prj.AngN) == (7, 5, 3)
+    assert not a.prj_data
+    b = mtr.AxisData(coef, coef, np.zeros((3, 5, 7), np.float32)).c_struct()
+    assert b.prj_data
+
+
 def test_no_device_reports_status():
     import torch
 
