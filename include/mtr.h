@@ -98,6 +98,10 @@ typedef struct mtr_params {
  * in device memory: volumes larger than HBM.  No counterpart in the
  * reference, which splits Z over MPI ranks (MpiBigData.cpp). */
 #define MTR_FLAG_HOST_VOLUMES 4
+/* Keep the FP64 convergence record of the MACE loop (mtr_recon_changes): the
+ * relative change of the consensus per outer iteration, two FP64 sums per
+ * voxel in the MACE step.  mtr_recon_run_until turns it on by itself. */
+#define MTR_FLAG_RECORD_CHANGES 8
 
 /* Fill p with the reference defaults (Options(), ReadAndInitialOptions.h:33-42). */
 void mtr_params_default(mtr_params* p);
@@ -126,6 +130,21 @@ mtr_status mtr_context_trim(mtr_context* ctx);
 /* Number of libmtr kernel launches issued by this process so far (graph
  * replays count every kernel node). */
 mtr_status mtr_context_launch_count(const mtr_context* ctx, long long* out);
+/* Of those, the launches of the TMA-windowed projector kernels: the
+ * back-projection gather and the forward splat that stage detector windows
+ * in shared memory (counted when issued; graph replays are not counted). */
+mtr_status mtr_context_windowed_launch_count(const mtr_context* ctx, long long* out);
+/* Failure-path hook, process-wide: the number of polls after which the
+ * pipeline waits of the windowed back-projection (the producer waiting for a
+ * free window stage, the consumers for a loaded window) give up, flag the
+ * launch and return; the kernel still waits for its own copies in flight
+ * before it exits.  A flagged run makes mtr_recon_check (and the host-buffer
+ * downloads) report MTR_ERR_TIMEOUT; the context stays usable.  Negative
+ * restores the default (2^24 polls); 0 makes every such wait give up at once.
+ * Read when a launch is issued (a captured graph keeps the value it was
+ * captured with).  The reference has no bounded waits (it only prints
+ * kernel errors, FunctionOnGPU.cu:3-10). */
+mtr_status mtr_set_wait_limit(long long polls);
 
 /* Kernel classes for per-kernel timing. */
 #define MTR_KERNEL_WBP 0
@@ -169,11 +188,17 @@ mtr_status mtr_sirt(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol,
  * (AngN*Y*X floats, x fastest) and slab_dev (X*Y*(slice_end-slice_start)
  * floats, updated in place), enqueued on the context stream.  The working
  * arrays live in one fixed device array of MTR_NOALLOC_SCRATCH_FLOATS floats
- * (32 MiB) compiled into the library and held by every GPU that loads it:
- * 3*AngN*Y*X + X*Y*(slice_end-slice_start) must not exceed it, else
- * MTR_ERR_CAPACITY.  All calls share that array: calls that overlap on the
- * GPU race, so issue them in order on one stream.  The first call on a device
- * looks up the array's device address; make it before any stream capture. */
+ * (32 MiB) compiled into the library: 3*AngN*Y*X + X*Y*(slice_end-slice_start)
+ * must not exceed it, else MTR_ERR_CAPACITY.  The CUDA runtime loads a
+ * library's device code lazily (the default since CUDA 12.2), so the array is
+ * placed on a device by the first call there, which looks up its device
+ * address; from then on the device holds it until the process exits.  That
+ * first call can therefore still allocate (and fail when the device is out of
+ * memory): make it at start-up, outside the stage that must not allocate, and
+ * before any stream capture (a call with n_inner = 0 does only the set-up and
+ * the geometry sums), or run with CUDA_MODULE_LOADING=EAGER.  All calls share
+ * that array: calls that overlap on the GPU race, so issue them in order on
+ * one stream. */
 #define MTR_NOALLOC_SCRATCH_FLOATS (8 * 1024 * 1024)
 mtr_status mtr_sirt_noalloc(mtr_context* ctx, mtr_projection_size prj, const double* x_coef_dev,
                             const double* y_coef_dev, const float* prj_dev, mtr_volume_size vol, int slice_start,
@@ -256,7 +281,7 @@ mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind);
 /* Squared residual norms, n_outer*K*n_inner doubles (MTR_FLAG_RECORD_NORMS). */
 mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n);
 /* FP64 convergence record of the MACE loop, computed on the GPU by the MACE
- * step: out[it] = ||w_avg(it) - w_avg(it-1)|| / ||w_avg(it)||, the relative
+ * step when MTR_FLAG_RECORD_CHANGES is set (else MTR_ERR_INVALID_ARGUMENT): out[it] = ||w_avg(it) - w_avg(it-1)|| / ||w_avg(it)||, the relative
  * L2 change of the consensus in outer iteration it (w_avg(-1) = the WBP
  * init), for the first min(n, n_outer) iterations (0 for iterations not run).
  * The reference has no convergence test (fixed iteration counts,

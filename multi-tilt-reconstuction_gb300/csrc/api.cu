@@ -22,6 +22,7 @@ using namespace mtr;
 // ---------------------------------------------------------------------------
 
 std::atomic<long long> mtr::g_launches{0};
+std::atomic<long long> mtr::g_windowed_launches{0};
 
 namespace {
 
@@ -149,6 +150,18 @@ mtr_status mtr_context_launch_count(const mtr_context* ctx, long long* out) {
   if (!out) return MTR_ERR_INVALID_ARGUMENT;
   (void)ctx;
   *out = g_launches.load();
+  return MTR_OK;
+}
+
+mtr_status mtr_set_wait_limit(long long polls) {
+  set_pipeline_wait_limit(polls);
+  return MTR_OK;
+}
+
+mtr_status mtr_context_windowed_launch_count(const mtr_context* ctx, long long* out) {
+  if (!out) return MTR_ERR_INVALID_ARGUMENT;
+  (void)ctx;
+  *out = g_windowed_launches.load();
   return MTR_OK;
 }
 

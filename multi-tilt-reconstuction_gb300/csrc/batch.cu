@@ -191,22 +191,17 @@ mtr_status mtr::enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, in
   constexpr int kSides = 8;
   const bool par = !t.own.empty() && !ctx->profiling;
   const int sides = par ? std::min<int>(kSides, (int)t.own.size()) : 0;
+  ForkJoin fj(ctx);  // joined back to the context stream on every exit path
   if (par) {
-    cudaEvent_t fork = ctx->sync_event(0);
-    if (!fork) return set_error(ctx, MTR_ERR_CUDA, "event creation");
-    MTR_CK(ctx, cudaEventRecord(fork, st));
-    for (int i = 0; i < sides; ++i) {
-      cudaStream_t si = ctx->side_stream(i);
-      if (!si) return set_error(ctx, MTR_ERR_CUDA, "side stream creation");
-      MTR_CK(ctx, cudaStreamWaitEvent(si, fork, 0));
-    }
+    const mtr_status s = fj.fork(sides);
+    if (s != MTR_OK) return s;
   }
   for (size_t i = 0; i < t.own.size(); ++i) {
-    if (par) ctx->stream = ctx->side_stream((int)(i % (size_t)sides));
+    if (par) fj.use((int)(i % (size_t)sides));
     mtr_status s = recon_enqueue_forward(t.own[i].first, t.own[i].second);
     if (s == MTR_OK) s = recon_enqueue_residual(t.own[i].first, t.own[i].second);
     if (s == MTR_OK) s = recon_enqueue_sirt_bp(t.own[i].first, t.own[i].second);
-    ctx->stream = st;
+    fj.use(-1);
     if (s != MTR_OK) return s;
   }
   {
@@ -240,15 +235,7 @@ mtr_status mtr::enqueue_sirt_iteration(mtr_context* ctx, const SirtTables& t, in
       if (e != cudaSuccess) return cuda_error(ctx, e, "batched back-projection");
     }
   }
-  if (par) {
-    for (int i = 0; i < sides; ++i) {
-      cudaEvent_t join = ctx->sync_event(1 + i);
-      if (!join) return set_error(ctx, MTR_ERR_CUDA, "event creation");
-      MTR_CK(ctx, cudaEventRecord(join, ctx->side_stream(i)));
-      MTR_CK(ctx, cudaStreamWaitEvent(st, join, 0));
-    }
-  }
-  return MTR_OK;
+  return MTR_OK;  // (fj joins the side streams)
 }
 
 struct mtr_batch {
@@ -312,28 +299,17 @@ mtr_status enqueue_batch(mtr_batch* b) {
   constexpr int kSides = 8;
   const bool par = b->rec.size() > 1 && !ctx->profiling;
   const int sides = par ? std::min<int>(kSides, (int)b->rec.size()) : 0;
-  if (par) {
-    cudaEvent_t fork = ctx->sync_event(0);
-    if (!fork) return set_error(ctx, MTR_ERR_CUDA, "event creation");
-    MTR_CK(ctx, cudaEventRecord(fork, st));
-    for (int i = 0; i < sides; ++i) {
-      cudaStream_t si = ctx->side_stream(i);
-      if (!si) return set_error(ctx, MTR_ERR_CUDA, "side stream creation");
-      MTR_CK(ctx, cudaStreamWaitEvent(si, fork, 0));
+  {
+    ForkJoin fj(ctx);  // joined back to the context stream on every exit path
+    if (par) {
+      const mtr_status s = fj.fork(sides);
+      if (s != MTR_OK) return s;
     }
-  }
-  for (size_t i = 0; i < b->rec.size(); ++i) {
-    if (par) ctx->stream = ctx->side_stream((int)(i % (size_t)sides));
-    const mtr_status s = recon_enqueue_init(b->rec[i]);
-    ctx->stream = st;
-    if (s != MTR_OK) return s;
-  }
-  if (par) {
-    for (int i = 0; i < sides; ++i) {
-      cudaEvent_t join = ctx->sync_event(1 + i);
-      if (!join) return set_error(ctx, MTR_ERR_CUDA, "event creation");
-      MTR_CK(ctx, cudaEventRecord(join, ctx->side_stream(i)));
-      MTR_CK(ctx, cudaStreamWaitEvent(st, join, 0));
+    for (size_t i = 0; i < b->rec.size(); ++i) {
+      if (par) fj.use((int)(i % (size_t)sides));
+      const mtr_status s = recon_enqueue_init(b->rec[i]);
+      fj.use(-1);
+      if (s != MTR_OK) return s;
     }
   }
   for (int it = 0; it < b->p.iter_times; ++it) {
@@ -357,6 +333,16 @@ mtr_status mtr_batch_create(mtr_context* ctx, int n, const mtr_instance* inst, c
                             mtr_batch** out) {
   if (!ctx || !inst || !params || !out || n <= 0) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "invalid argument");
   *out = nullptr;
+  // The batch API has no upload call: every axis of every instance must bring
+  // its projections.
+  for (int i = 0; i < n; ++i) {
+    if (!inst[i].axes || inst[i].n_axes <= 0 || inst[i].n_axes > MTR_MAX_AXES)
+      return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "instance: null axes or axis count out of range");
+    for (int k = 0; k < inst[i].n_axes; ++k) {
+      const mtr_status sa = check_axis(ctx, inst[i].axes[k], true);
+      if (sa != MTR_OK) return sa;
+    }
+  }
   DeviceGuard g(ctx->device);
   std::unique_ptr<mtr_batch> b(new (std::nothrow) mtr_batch());
   if (!b) return set_error(ctx, MTR_ERR_OUT_OF_MEMORY, "host allocation");

@@ -18,6 +18,8 @@
 //
 // All mbarrier waits are bounded; a wait that gives up sets *err and the CTA
 // drains its own in-flight copies (bounded) before returning.
+#include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "mtr_internal.h"
@@ -29,7 +31,12 @@ namespace {
 constexpr int NST = 4;             // pipeline stages
 constexpr int kConsumerWarps = 8;  // 256 consumer threads
 constexpr int kThreads = (kConsumerWarps + 1) * 32;
-constexpr uint32_t kWaitIters = 1u << 24;
+// Polls of the pipeline waits (producer on a free stage, consumers on a
+// loaded window) before they give up; a launch argument, so that a test can
+// make them give up at once.  The drain of the producer's own copies in
+// flight always has the full bound: a CTA never exits with a copy pending.
+constexpr uint32_t kDrainIters = 1u << 24;
+std::atomic<unsigned> g_wait_iters{1u << 24};
 constexpr float kMagic = 12582912.0f;  // 1.5 * 2^23: x + kMagic holds round(x) in its low bits
 constexpr int kMagicBits = 0x4B400000;
 
@@ -53,6 +60,7 @@ struct BpArgs {
   void* vol_copy;
   int copy_kind;
   int* err;
+  unsigned wait_iters;  // polls of a pipeline wait before it gives up
 };
 
 template <typename PT> __device__ __forceinline__ float to_f(PT v);
@@ -194,7 +202,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
       for (int a = 0; a < A; ++a) {
         const int s = a % NST;
         const int n = a / NST;
-        if (n > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((n - 1) & 1), kWaitIters)) {
+        if (n > 0 && !mbar_wait_bounded(&empty[s], (uint32_t)((n - 1) & 1), P.wait_iters)) {
           atomicExch(P.err, 2);
           break;
         }
@@ -207,7 +215,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
       // (earlier ones into that stage completed before it could be reissued).
       for (int s = 0; s < NST && s < issued; ++s) {
         const int n_last = (issued - 1 - s) / NST;
-        if (!mbar_wait_bounded(&full[s], (uint32_t)(n_last & 1), kWaitIters)) atomicExch(P.err, 3);
+        if (!mbar_wait_bounded(&full[s], (uint32_t)(n_last & 1), kDrainIters)) atomicExch(P.err, 3);
       }
     }
     return;
@@ -228,7 +236,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   for (int a = 0; a < A; ++a) {
     const int st = a % NST;
     // every lane of the warp takes the same branch (the warp syncs below)
-    if (!__all_sync(0xffffffffu, mbar_wait_bounded(&full[st], (uint32_t)((a / NST) & 1), kWaitIters))) {
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(&full[st], (uint32_t)((a / NST) & 1), P.wait_iters))) {
       if (lane == 0) atomicExch(P.err, 4);
       break;
     }
@@ -392,7 +400,9 @@ cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cud
   const int BX = LANES == 1 ? kConsumerWarps : 32, BY = LANES == 1 ? 32 : kConsumerWarps;
   const dim3 grid((P.vol.NX + BX - 1) / BX, (P.z1 - P.z0 + NZ - 1) / NZ, (P.vol.NY + BY - 1) / BY);
   kern<<<grid, kThreads, smem, st>>>(map, P);
-  return cudaGetLastError();
+  const cudaError_t le = cudaGetLastError();
+  if (le == cudaSuccess) g_windowed_launches.fetch_add(1, std::memory_order_relaxed);
+  return le;
 }
 
 template <typename PT, int MODE, int LANES, bool BZ0>
@@ -435,7 +445,7 @@ __device__ __forceinline__ void bp_batch_item(const CUtensorMap* map, const BpAr
 
 __global__ void __launch_bounds__(kThreads, 5)
 bp_batch_kernel(const BpBatchDesc* __restrict__ descs, const long long* __restrict__ first, int n_desc,
-                long long n_items, int* err) {
+                long long n_items, int* err, unsigned wait_iters) {
   extern __shared__ __align__(128) unsigned char smem[];
   // The item's arguments are staged in shared memory: read from there (like
   // the constant bank of a single launch) they cost no registers.
@@ -448,7 +458,7 @@ bp_batch_kernel(const BpBatchDesc* __restrict__ descs, const long long* __restri
       const int2 item = work_item(first, n_desc, it);
       const BpBatchDesc& D = descs[item.x];
       sP = BpArgs{D.ax, D.vol, D.vol.Zs, D.vol.Zs + D.vol.NZ, D.WX, D.WY, D.align, 1, D.step, D.vol_out,
-                  const_cast<float*>(D.cbp), D.vol_copy, D.copy_kind, err};
+                  const_cast<float*>(D.cbp), D.vol_copy, D.copy_kind, err, wait_iters};
       sMap = D.map;
       const int gz = (D.vol.NZ + D.nz - 1) / D.nz;  // x fastest, then z, then y (as bp_tma_kernel)
       sB[0] = item.y % D.gx;
@@ -481,8 +491,16 @@ cudaError_t launch_backproject_batch(const BpBatchDesc* descs, const long long* 
                                      size_t smem, int grid, int* err, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(bp_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  bp_batch_kernel<<<grid, kThreads, smem, st>>>(descs, first, n_desc, n_items, err);
-  return cudaGetLastError();
+  bp_batch_kernel<<<grid, kThreads, smem, st>>>(descs, first, n_desc, n_items, err,
+                                                 g_wait_iters.load(std::memory_order_relaxed));
+  const cudaError_t le = cudaGetLastError();
+  if (le == cudaSuccess) g_windowed_launches.fetch_add(1, std::memory_order_relaxed);
+  return le;
+}
+
+void set_pipeline_wait_limit(long long polls) {
+  g_wait_iters.store(polls < 0 ? (1u << 24) : (unsigned)std::min<long long>(polls, 0xffffffffLL),
+                     std::memory_order_relaxed);
 }
 
 // Mean number of shared-memory wavefronts per tap load of one warp for a
@@ -609,7 +627,9 @@ template <typename PT>
 cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, const AxisDev& ax, const VolDev& vol,
                                    int mode, float step, float* vol_out, float* cbp, void* vol_copy, int copy_kind,
                                    int z0, int z1, int* err, cudaStream_t st) {
-  BpArgs P{ax, vol, z0, z1, plan.WX, plan.WY, plan.align, mode, step, vol_out, cbp, vol_copy, copy_kind, err};
+  BpArgs P{ax,        vol,      z0,       z1,   plan.WX, plan.WY, plan.align,
+           mode,      step,     vol_out,  cbp,  vol_copy, copy_kind, err,
+           g_wait_iters.load(std::memory_order_relaxed)};
   if (mode == 0) {
     if (plan.lanes == 2) return plan.bz0 ? launch_nz<PT, 0, 2, true>(map, P, plan, st)
                                          : launch_nz<PT, 0, 2, false>(map, P, plan, st);

@@ -3,7 +3,9 @@
 // (initialZdata) and mtr_update_w (runMaceOnGPU / runMaceOnCPU).
 // Like the reference they upload, compute and download per call; unlike it
 // they keep the whole SIRT loop on the device (no per-iteration host
-// residual, no MPI) and return a status instead of exiting.
+// residual, no MPI) and return a status instead of exiting.  mtr_wbp and
+// mtr_sirt run on a one-axis reconstruction object over the slab, so they use
+// the autotuned, TMA-windowed projectors and the context's memory pool.
 #include "mtr_internal.h"
 #include "mtr_runtime.h"
 
@@ -17,22 +19,30 @@ mtr_status check_slab(mtr_context* ctx, const mtr_volume_size& vol, int z0, int 
   return MTR_OK;
 }
 
-struct AxisUpload {
-  DevBuf xc, yc, b;
-  AxisDev dev;
+// A one-axis FP32 reconstruction object whose volume frame is the Z-slab
+// [z0, z1) of vol: the same arrays (from the context's pool), autotuned tiles
+// and kernels as mtr_recon_create, so the reference-shaped calls run the
+// TMA-windowed projectors wherever the windows fit.  Destroyed with the
+// object, which waits for the work that used its arrays.
+struct SlabRecon {
+  mtr_recon* r = nullptr;
+  mtr_status create(mtr_context* ctx, const mtr_axis& axis, const mtr_volume_size& vol, int z0, int z1, int n_inner,
+                    float step) {
+    mtr_volume_size sv = vol;
+    sv.Zstart = z0;
+    sv.Zend = z1;
+    sv.Z = z1 - z0;
+    mtr_params p;
+    mtr_params_default(&p);
+    p.iter_times = 1;
+    p.sirt_inner = n_inner;
+    p.sirt_step = step;
+    p.precision = MTR_PREC_FP32;
+    p.flags = 0;
+    return mtr_recon_create(ctx, 1, &axis, sv, &p, MTR_MEM_HOST, &r);
+  }
+  ~SlabRecon() { mtr_recon_destroy(r); }
 };
-
-mtr_status upload_axis(mtr_context* ctx, const mtr_axis& a, AxisUpload& u) {
-  const long long np = (long long)a.prj.X * a.prj.Y * a.prj.AngN;
-  MTR_CK(ctx, u.xc.alloc(sizeof(double) * 4 * a.prj.AngN));
-  MTR_CK(ctx, u.yc.alloc(sizeof(double) * 4 * a.prj.AngN));
-  MTR_CK(ctx, u.b.alloc((size_t)np * 4));
-  MTR_CK(ctx, cudaMemcpyAsync(u.xc.p, a.x_coef, sizeof(double) * 4 * a.prj.AngN, cudaMemcpyHostToDevice, ctx->stream));
-  MTR_CK(ctx, cudaMemcpyAsync(u.yc.p, a.y_coef, sizeof(double) * 4 * a.prj.AngN, cudaMemcpyHostToDevice, ctx->stream));
-  MTR_CK(ctx, cudaMemcpyAsync(u.b.p, a.prj_data, (size_t)np * 4, cudaMemcpyHostToDevice, ctx->stream));
-  u.dev = AxisDev{a.prj.X, a.prj.Y, a.prj.AngN, u.xc.as<double>(), u.yc.as<double>(), a.prj.X};
-  return MTR_OK;
-}
 
 }  // namespace
 
@@ -46,20 +56,15 @@ mtr_status mtr_wbp(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol, 
   if (s == MTR_OK) s = check_slab(ctx, vol, slice_start, slice_end);
   if (s != MTR_OK) return s;
   DeviceGuard g(ctx->device);
-  AxisUpload u;
-  s = upload_axis(ctx, *axis, u);
+  SlabRecon sr;
+  s = sr.create(ctx, *axis, vol, slice_start, slice_end, 0, 0.f);
   if (s != MTR_OK) return s;
-  const long long ns = (long long)vol.X * vol.Y * (slice_end - slice_start);
-  DevBuf x, cbp;
-  MTR_CK(ctx, x.alloc((size_t)ns * 4));
-  MTR_CK(ctx, cbp.alloc((size_t)ns * 4));
-  const VolDev v{vol.Xstart, vol.Ystart, slice_start, vol.X, vol.Y, slice_end - slice_start};
-  launch_backproject<float>(u.dev, v, u.b.as<float>(), 0, 0.f, x.as<float>(), cbp.as<float>(), nullptr, 0,
-                            slice_start, slice_end, ctx->stream);
-  MTR_CK_LAUNCH(ctx, "wbp");
-  MTR_CK(ctx, cudaMemcpyAsync(slab_out, x.p, (size_t)ns * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  mtr_recon* r = sr.r;
+  s = recon_enqueue_wbp(r, 0);  // x = s/c, cbp = c over the slab
+  if (s != MTR_OK) return s;
+  MTR_CK(ctx, cudaMemcpyAsync(slab_out, r->ax[0].x.p, (size_t)r->nv * 4, cudaMemcpyDeviceToHost, ctx->stream));
   MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  return MTR_OK;
+  return mtr_recon_check(r);
 }
 
 mtr_status mtr_sirt(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol, int slice_start, int slice_end,
@@ -71,40 +76,25 @@ mtr_status mtr_sirt(mtr_context* ctx, const mtr_axis* axis, mtr_volume_size vol,
   if (s == MTR_OK) s = check_slab(ctx, vol, slice_start, slice_end);
   if (s != MTR_OK) return s;
   DeviceGuard g(ctx->device);
-  AxisUpload u;
-  s = upload_axis(ctx, *axis, u);
+  SlabRecon sr;
+  s = sr.create(ctx, *axis, vol, slice_start, slice_end, n_inner, sirt_step);
   if (s != MTR_OK) return s;
-  const long long np = (long long)axis->prj.X * axis->prj.Y * axis->prj.AngN;
-  const long long ns = (long long)vol.X * vol.Y * (slice_end - slice_start);
-  DevBuf x, cbp, sbuf, cf, r;
-  MTR_CK(ctx, x.alloc((size_t)ns * 4));
-  MTR_CK(ctx, cbp.alloc((size_t)ns * 4));
-  MTR_CK(ctx, sbuf.alloc((size_t)np * 4));
-  MTR_CK(ctx, cf.alloc((size_t)np * 4));
-  MTR_CK(ctx, r.alloc((size_t)np * 4));
-  MTR_CK(ctx, cudaMemcpyAsync(x.p, slab_inout, (size_t)ns * 4, cudaMemcpyHostToDevice, ctx->stream));
-  MTR_CK(ctx, cudaMemsetAsync(sbuf.p, 0, (size_t)np * 4, ctx->stream));
-  MTR_CK(ctx, cudaMemsetAsync(cf.p, 0, (size_t)np * 4, ctx->stream));
-  const VolDev v{vol.Xstart, vol.Ystart, slice_start, vol.X, vol.Y, slice_end - slice_start};
-  // Geometry-only sums, once (the reference recomputes c every iteration).
-  launch_forward<float>(u.dev, v, nullptr, cf.as<float>(), slice_start, slice_end, ctx->stream);
-  MTR_CK_LAUNCH(ctx, "forward row sums");
-  launch_backproject<float>(u.dev, v, u.b.as<float>(), 2, 0.f, nullptr, cbp.as<float>(), nullptr, 0, slice_start,
-                            slice_end, ctx->stream);
-  MTR_CK_LAUNCH(ctx, "back-projection weight sums");
+  mtr_recon* r = sr.r;
+  // The WBP pass yields the back-projection weight sums C = A^T 1 of the slab
+  // (geometry only; the reference recomputes its sums every call and every
+  // iteration, FunctionOnGPU.cu:218-232); its volume is then replaced by the
+  // caller's slab.
+  s = recon_enqueue_wbp(r, 0);
+  if (s != MTR_OK) return s;
+  MTR_CK(ctx, cudaMemcpyAsync(r->ax[0].x.p, slab_inout, (size_t)r->nv * 4, cudaMemcpyHostToDevice, ctx->stream));
   for (int it = 0; it < n_inner; ++it) {
-    launch_forward<float>(u.dev, v, x.as<float>(), sbuf.as<float>(), slice_start, slice_end, ctx->stream);
-    MTR_CK_LAUNCH(ctx, "forward splat");
-    launch_residual<float, float>(np, u.b.as<float>(), sbuf.as<float>(), cf.as<float>(), r.as<float>(), nullptr,
-                                  ctx->stream);
-    MTR_CK_LAUNCH(ctx, "residual");
-    launch_backproject<float>(u.dev, v, r.as<float>(), 1, sirt_step, x.as<float>(), cbp.as<float>(), nullptr, 0,
-                              slice_start, slice_end, ctx->stream);
-    MTR_CK_LAUNCH(ctx, "sirt back-projection");
+    if ((s = recon_enqueue_forward(r, 0)) != MTR_OK) return s;
+    if ((s = recon_enqueue_residual(r, 0)) != MTR_OK) return s;
+    if ((s = recon_enqueue_sirt_bp(r, 0)) != MTR_OK) return s;
   }
-  MTR_CK(ctx, cudaMemcpyAsync(slab_inout, x.p, (size_t)ns * 4, cudaMemcpyDeviceToHost, ctx->stream));
+  MTR_CK(ctx, cudaMemcpyAsync(slab_inout, r->ax[0].x.p, (size_t)r->nv * 4, cudaMemcpyDeviceToHost, ctx->stream));
   MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
-  return MTR_OK;
+  return mtr_recon_check(r);
 }
 
 static mtr_status elementwise(mtr_context* ctx, mtr_volume_size vol, const float* a, const float* b, float* io,

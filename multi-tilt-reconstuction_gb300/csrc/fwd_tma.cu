@@ -416,7 +416,9 @@ cudaError_t launch_one(const CUtensorMap& map, FwdArgs P, size_t smem, int num_s
   P.max_angles = (P.ax.A + groups - 1) / groups;
   const dim3 grid((P.vol.NX + BX - 1) / BX, (P.vol.NY + BY - 1) / BY, ((P.z1 - P.z0 + NZ - 1) / NZ) * groups);
   kern<<<grid, kThreads, smem, st>>>(map, P);
-  return cudaGetLastError();
+  const cudaError_t le = cudaGetLastError();
+  if (le == cudaSuccess) g_windowed_launches.fetch_add(1, std::memory_order_relaxed);
+  return le;
 }
 
 // Z-dependent y-maps take the per-tap path and use one depth.
@@ -503,7 +505,9 @@ cudaError_t launch_forward_batch(const FwdBatchDesc* descs, const long long* fir
   cudaError_t e = cudaFuncSetAttribute(fwd_batch_kernel<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   fwd_batch_kernel<VT><<<grid, kThreads, smem, st>>>(descs, first, n_desc, n_items);
-  return cudaGetLastError();
+  const cudaError_t le = cudaGetLastError();
+  if (le == cudaSuccess) g_windowed_launches.fetch_add(1, std::memory_order_relaxed);
+  return le;
 }
 
 template int forward_batch_ctas_per_sm<float>(size_t);
@@ -596,8 +600,7 @@ FwdPlan plan_forward(const std::vector<double>& xc, const std::vector<double>& y
 template <typename VT>
 cudaError_t launch_forward_tma(const CUtensorMap& smap, const FwdPlan& plan, const AxisDev& ax, const VolDev& vol,
                                const VT* x, int z0, int z1, int* err, cudaStream_t st) {
-  int dev = 0, sms = 152;
-  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = device_sm_count();
   FwdArgs P{ax, vol, z0, z1, plan.WX, plan.WY, 1, ax.A, plan.mass_shift, x, err};
   if (plan.lanes == 2) return plan.bz0 ? launch_nz<VT, 2, true>(smap, P, plan, sms, st)
                                        : launch_nz<VT, 2, false>(smap, P, plan, sms, st);

@@ -1,5 +1,7 @@
 // Elementwise and MACE consensus kernels (sm_103a).  These are HBM-bound:
 // grid-stride loops over the volume, sized to a multiple of the SM count.
+#include <atomic>
+
 #include "mtr_internal.h"
 
 namespace mtr {
@@ -9,7 +11,7 @@ constexpr int kThreads = 256;
 
 unsigned grid_for(long long n) {
   long long b = (n + kThreads - 1) / kThreads;
-  const long long cap = 152LL * 8;  // 8 resident CTAs per SM on 152 SMs
+  const long long cap = (long long)device_sm_count() * 8;  // 8 resident CTAs per SM
   if (b > cap) b = cap;
   if (b < 1) b = 1;
   return (unsigned)b;
@@ -175,6 +177,27 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __re
 }
 
 }  // namespace
+
+int device_sm_count() {
+  constexpr int kMaxDevices = 64;
+  static std::atomic<int> cached[kMaxDevices];  // 0 = not yet queried
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    dev = -1;
+  }
+  if (dev >= 0) {
+    const int c = cached[dev].load(std::memory_order_relaxed);
+    if (c > 0) return c;
+  }
+  int n = 0;
+  if (dev < 0 || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return 1;  // a one-SM grid still covers everything through its grid-stride loop
+  }
+  cached[dev].store(n, std::memory_order_relaxed);
+  return n;
+}
 
 void launch_mace_batch(const MaceBatchDesc* descs, const long long* first, int n_desc, long long n_items, int grid,
                        cudaStream_t st) {

@@ -1,6 +1,7 @@
 // Internal declarations shared by the CUDA translation units of libmtr.
 #pragma once
 
+#include <atomic>
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
@@ -15,6 +16,11 @@
 #include "../../include/mtr.h"
 
 namespace mtr {
+
+// Process-wide count of launches of the TMA-windowed projector kernels (the
+// back-projection gather and the forward splat that stage detector windows in
+// shared memory), single and persistent, counted when they are issued.
+extern std::atomic<long long> g_windowed_launches;
 
 // Maximum number of projection angles per tilt axis handled by one launch.
 // The per-angle constants of a CTA live in shared memory (10 words/angle).
@@ -128,6 +134,10 @@ cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, c
                                    const VolDev& vol, int mode, float step, float* vol_out, float* cbp,
                                    void* vol_copy, int copy_kind, int z0, int z1, int* err, cudaStream_t st);
 
+// Polls a pipeline wait of the windowed back-projection makes before it
+// gives up and flags the launch (negative: the default, 2^24); read at launch.
+void set_pipeline_wait_limit(long long polls);
+
 // 3-D tiled tensor map over [depth][height][pitch] fp32/fp16 elements with
 // logical width `width`, box (bw, bh, 1), zero fill (bp_tma.cu).
 bool encode_tensor_map_3d(CUtensorMap* map, const void* base, bool half, int width, int pitch, int height, int depth,
@@ -224,6 +234,8 @@ void launch_mace_batch(const MaceBatchDesc* descs, const long long* first, int n
                        cudaStream_t st);
 
 // ---- elementwise / MACE (mace.cu) ----------------------------------------
+// Streaming multiprocessors of the current device (queried once per device).
+int device_sm_count();
 void launch_fill(float* p, long long n, float v, cudaStream_t st);
 void launch_axpy_acc(float* dst, const float* src, long long n, cudaStream_t st);  // dst += src
 // Fused MACE step over K axes (see mace.cu).

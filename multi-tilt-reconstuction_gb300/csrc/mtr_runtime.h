@@ -122,6 +122,46 @@ mtr_status check_volume(mtr_context* ctx, const mtr_volume_size& v);
 // data_required false: prj_data may be null (projections uploaded later).
 mtr_status check_axis(mtr_context* ctx, const mtr_axis& a, bool data_required = true);
 
+// Side streams forked from the context stream and joined back to it.
+// fork(n) makes side streams 0..n-1 wait for the work enqueued so far on the
+// context stream; use(i) points the context at side stream i (use(-1) at the
+// context stream).  The destructor, on every exit path, records a join event
+// on each forked side stream, makes the context stream wait for it and
+// restores the context stream: an error return in the middle of a section
+// never leaves a stream capture with unjoined work, and later work on the
+// context stream is ordered after everything the side streams received.
+struct ForkJoin {
+  mtr_context* ctx;
+  cudaStream_t main;
+  int forked = 0;
+  explicit ForkJoin(mtr_context* c) : ctx(c), main(c->stream) {}
+  ForkJoin(const ForkJoin&) = delete;
+  ForkJoin& operator=(const ForkJoin&) = delete;
+  mtr_status fork(int n) {
+    cudaEvent_t f = ctx->sync_event(0);
+    if (!f) return set_error(ctx, MTR_ERR_CUDA, "event creation");
+    cudaError_t e = cudaEventRecord(f, main);
+    if (e != cudaSuccess) return cuda_error(ctx, e, "cudaEventRecord(fork)");
+    for (int i = forked; i < n; ++i) {
+      cudaStream_t s = ctx->side_stream(i);
+      if (!s || !ctx->sync_event(1 + i)) return set_error(ctx, MTR_ERR_CUDA, "side stream creation");
+      e = cudaStreamWaitEvent(s, f, 0);
+      if (e != cudaSuccess) return cuda_error(ctx, e, "cudaStreamWaitEvent(fork)");
+      forked = i + 1;
+    }
+    return MTR_OK;
+  }
+  void use(int i) { ctx->stream = i < 0 ? main : ctx->side_streams[(size_t)i]; }
+  ~ForkJoin() {
+    ctx->stream = main;
+    for (int i = 0; i < forked; ++i) {
+      cudaEvent_t join = ctx->sync_event(1 + i);
+      cudaEventRecord(join, ctx->side_streams[(size_t)i]);
+      cudaStreamWaitEvent(main, join, 0);
+    }
+  }
+};
+
 // Makes a device current for a scope and restores the previous one.
 struct DeviceGuard {
   int prev = -1;
@@ -273,6 +313,8 @@ struct mtr_recon;
 namespace mtr {
 // WBP sum into w_avg, w_k = z_k = w_avg, records reset (recon.cu).
 mtr_status recon_enqueue_init(mtr_recon* r);
+// WBP of axis k alone: x_k = s/c and the weight sums cbp_k = c.
+mtr_status recon_enqueue_wbp(mtr_recon* r, int k);
 // One SIRT phase of axis k of a reconstruction, with its own kernels.
 mtr_status recon_enqueue_forward(mtr_recon* r, int k);
 mtr_status recon_enqueue_residual(mtr_recon* r, int k);
@@ -315,6 +357,7 @@ struct mtr_recon {
   mtr::DevBuf err;        // device error flag written by bounded waits (int)
   long long bytes = 0;
   bool geometry_ready = false;  // cf and cbp computed
+  bool record_changes = false;  // MACE steps accumulate the FP64 convergence record
   int outer_done = 0;           // MACE outer iterations the state has been through
   cudaGraphExec_t graph = nullptr;
   long long graph_nodes = 0;

@@ -323,7 +323,8 @@ void launch_forward(const AxisDev& ax, const VolDev& vol, const VT* x, float* s,
 template <typename BT, typename RT>
 void launch_residual(long long n, const BT* b, float* s, const float* c, RT* r, double* norm2, cudaStream_t st) {
   long long blocks = (n / 4 + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;  // grid-stride loops cover the rest
+  const long long cap = (long long)device_sm_count() * 16;
+  if (blocks > cap) blocks = cap;  // grid-stride loops cover the rest
   if (blocks < 1) blocks = 1;
   static_assert(std::is_same<RT, float>::value, "the residual is FP32");
   // vector loads need 16-byte aligned arrays (caller-owned buffers may not be)

@@ -115,33 +115,51 @@ mtr_status enqueue_geometry(mtr_recon* r) {
   return MTR_OK;
 }
 
-mtr_status enqueue_forward(mtr_recon* r, AxisState& a) {
+// The Z planes [z0, z1) one launch works on and the arrays that hold exactly
+// those planes: an axis' whole device arrays, or one slot of a streamed
+// reconstruction's device working set.
+struct VolSpan {
+  int z0, z1;
+  float* x;     // SIRT iterate (the WBP writes it)
+  float* cbp;   // back-projection weight sums
+  void* xcopy;  // BF16 / FP16 copy of x read by the forward splat (mixed), or null
+};
+
+VolSpan whole_volume(const mtr_recon* r, AxisState& a) {
+  return VolSpan{r->vol.Zs, r->vol.Zs + r->vol.NZ, a.x.as<float>(), a.cbp.as<float>(), a.xcopy.p};
+}
+
+mtr_status enqueue_forward(mtr_recon* r, AxisState& a, const VolSpan& sp) {
   mtr_context* ctx = r->ctx;
   const VolDev& v = r->vol;
-  const int z0 = v.Zs, z1 = v.Zs + v.NZ;
+  const int z0 = sp.z0, z1 = sp.z1;
   ProfScope ps(ctx, MTR_KERNEL_FORWARD);
   if (a.ftma) {
     cudaError_t e;
     switch (copy_kind_of(r->p.precision)) {
-      case 1: e = launch_forward_tma<__nv_bfloat16>(a.map_s, a.fplan, a.dev(), v, a.xcopy.as<__nv_bfloat16>(), z0, z1,
+      case 1: e = launch_forward_tma<__nv_bfloat16>(a.map_s, a.fplan, a.dev(), v,
+                                                     static_cast<const __nv_bfloat16*>(sp.xcopy), z0, z1,
                                                      r->err.as<int>(), ctx->stream); break;
-      case 2: e = launch_forward_tma<__half>(a.map_s, a.fplan, a.dev(), v, a.xcopy.as<__half>(), z0, z1,
-                                              r->err.as<int>(), ctx->stream); break;
-      default: e = launch_forward_tma<float>(a.map_s, a.fplan, a.dev(), v, a.x.as<float>(), z0, z1,
-                                              r->err.as<int>(), ctx->stream); break;
+      case 2: e = launch_forward_tma<__half>(a.map_s, a.fplan, a.dev(), v, static_cast<const __half*>(sp.xcopy), z0,
+                                              z1, r->err.as<int>(), ctx->stream); break;
+      default: e = launch_forward_tma<float>(a.map_s, a.fplan, a.dev(), v, sp.x, z0, z1, r->err.as<int>(),
+                                              ctx->stream); break;
     }
     g_launches.fetch_add(1);
     if (e != cudaSuccess) return cuda_error(ctx, e, "forward splat (tma)");
     return MTR_OK;
   }
   switch (copy_kind_of(r->p.precision)) {
-    case 1: launch_forward<__nv_bfloat16>(a.dev(), v, a.xcopy.as<__nv_bfloat16>(), a.s.as<float>(), z0, z1, ctx->stream); break;
-    case 2: launch_forward<__half>(a.dev(), v, a.xcopy.as<__half>(), a.s.as<float>(), z0, z1, ctx->stream); break;
-    default: launch_forward<float>(a.dev(), v, a.x.as<float>(), a.s.as<float>(), z0, z1, ctx->stream); break;
+    case 1: launch_forward<__nv_bfloat16>(a.dev(), v, static_cast<const __nv_bfloat16*>(sp.xcopy), a.s.as<float>(),
+                                          z0, z1, ctx->stream); break;
+    case 2: launch_forward<__half>(a.dev(), v, static_cast<const __half*>(sp.xcopy), a.s.as<float>(), z0, z1,
+                                   ctx->stream); break;
+    default: launch_forward<float>(a.dev(), v, sp.x, a.s.as<float>(), z0, z1, ctx->stream); break;
   }
   MTR_CK_LAUNCH(ctx, "forward splat");
   return MTR_OK;
 }
+mtr_status enqueue_forward(mtr_recon* r, AxisState& a) { return enqueue_forward(r, a, whole_volume(r, a)); }
 
 mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
   mtr_context* ctx = r->ctx;
@@ -156,42 +174,52 @@ mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
   return MTR_OK;
 }
 
-mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const void* img_f32_or_null) {
+// Mixed precision: the windowed WBP gathers FP32 windows, so the FP16
+// projections are first widened into r (free until the first residual).
+mtr_status enqueue_widen_for_wbp(mtr_recon* r, AxisState& a) {
+  if (!(a.tma_b && mixed(r->p.precision))) return MTR_OK;
+  launch_widen(a.b.as<__half>(), a.r.as<float>(), a.np, r->ctx->stream);
+  MTR_CK_LAUNCH(r->ctx, "widen projections");
+  return MTR_OK;
+}
+
+// mode 0: WBP (x = s/c, cbp = c); mode 1: SIRT update from the residual.
+// widen: for the windowed mixed-precision WBP, widen the projections first
+// (a caller that runs several WBP spans of one axis widens them once).
+mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode, const VolSpan& sp, bool widen = true) {
   mtr_context* ctx = r->ctx;
   const VolDev& v = r->vol;
-  const int z0 = v.Zs, z1 = v.Zs + v.NZ;
+  const int z0 = sp.z0, z1 = sp.z1;
   const int ck = copy_kind_of(r->p.precision);
   ProfScope ps(ctx, mode == 0 ? MTR_KERNEL_WBP : MTR_KERNEL_BACKPROJECT);
   // WBP reads the projections (fp16 when mixed), SIRT reads the FP32 residual.
   const bool half_img = mode == 0 && mixed(r->p.precision);
-  if ((mode == 0 ? a.tma_b : a.tma) && !img_f32_or_null) {
-    if (half_img) {
-      launch_widen(a.b.as<__half>(), a.r.as<float>(), a.np, ctx->stream);
-      MTR_CK_LAUNCH(ctx, "widen projections");
+  if (mode == 0 ? a.tma_b : a.tma) {
+    if (half_img && widen) {
+      mtr_status s = enqueue_widen_for_wbp(r, a);
+      if (s != MTR_OK) return s;
     }
     cudaError_t e = launch_backproject_tma<float>(mode == 0 ? a.map_b : a.map_r, mode == 0 ? a.plan_b : a.plan,
-                                                  a.dev(), v, mode, r->p.sirt_step, a.x.as<float>(),
-                                                  a.cbp.as<float>(), a.xcopy.p, ck, z0, z1, r->err.as<int>(),
-                                                  ctx->stream);
+                                                  a.dev(), v, mode, r->p.sirt_step, sp.x, sp.cbp, sp.xcopy, ck, z0,
+                                                  z1, r->err.as<int>(), ctx->stream);
     g_launches.fetch_add(1);
     if (e != cudaSuccess) return cuda_error(ctx, e, "tma back-projection");
     return MTR_OK;
   }
   if (half_img) {
-    launch_backproject<__half>(a.dev(), v, a.b.as<__half>(), mode, r->p.sirt_step, a.x.as<float>(),
-                               a.cbp.as<float>(), a.xcopy.p, ck, z0, z1, ctx->stream);
+    launch_backproject<__half>(a.dev(), v, a.b.as<__half>(), mode, r->p.sirt_step, sp.x, sp.cbp, sp.xcopy, ck, z0,
+                               z1, ctx->stream);
   } else if (mixed(r->p.precision)) {
-    launch_backproject<float>(a.dev(), v, a.r.as<float>(), mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(),
-                              a.xcopy.p, ck, z0, z1, ctx->stream);
+    launch_backproject<float>(a.dev(), v, a.r.as<float>(), mode, r->p.sirt_step, sp.x, sp.cbp, sp.xcopy, ck, z0, z1,
+                              ctx->stream);
   } else {
     const float* img = mode == 0 ? a.b.as<float>() : a.r.as<float>();
-    if (img_f32_or_null) img = static_cast<const float*>(img_f32_or_null);
-    launch_backproject<float>(a.dev(), v, img, mode, r->p.sirt_step, a.x.as<float>(), a.cbp.as<float>(), nullptr, 0,
-                              z0, z1, ctx->stream);
+    launch_backproject<float>(a.dev(), v, img, mode, r->p.sirt_step, sp.x, sp.cbp, nullptr, 0, z0, z1, ctx->stream);
   }
   MTR_CK_LAUNCH(ctx, mode == 0 ? "wbp" : "sirt back-projection");
   return MTR_OK;
 }
+mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode) { return enqueue_bp(r, a, mode, whole_volume(r, a)); }
 
 }  // namespace
 
@@ -207,7 +235,7 @@ mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
   // Initial model: sum over axes of each axis' WBP (MultiAxis.cpp:181-200).
   MTR_CK(ctx, cudaMemsetAsync(wavg, 0, vbytes, ctx->stream));
   for (auto& a : r->ax) {
-    mtr_status s = enqueue_bp(r, a, 0, nullptr);
+    mtr_status s = enqueue_bp(r, a, 0);
     if (s != MTR_OK) return s;
     ProfScope ps(ctx, MTR_KERNEL_OTHER);
     launch_axpy_acc(wavg, a.x.as<float>(), nv, ctx->stream);
@@ -231,9 +259,10 @@ mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
   return MTR_OK;
 }
 
+mtr_status mtr::recon_enqueue_wbp(mtr_recon* r, int k) { return enqueue_bp(r, r->ax[k], 0); }
 mtr_status mtr::recon_enqueue_forward(mtr_recon* r, int k) { return enqueue_forward(r, r->ax[k]); }
 mtr_status mtr::recon_enqueue_residual(mtr_recon* r, int k) { return enqueue_residual(r, r->ax[k], nullptr); }
-mtr_status mtr::recon_enqueue_sirt_bp(mtr_recon* r, int k) { return enqueue_bp(r, r->ax[k], 1, nullptr); }
+mtr_status mtr::recon_enqueue_sirt_bp(mtr_recon* r, int k) { return enqueue_bp(r, r->ax[k], 1); }
 
 namespace {
 
@@ -247,7 +276,7 @@ mtr_status enqueue_axis_chain(mtr_recon* r, int k, int it) {
     if (s != MTR_OK) return s;
     s = enqueue_residual(r, a, norms && it < no ? norms + ((long long)it * K + k) * ni + j : nullptr);
     if (s != MTR_OK) return s;
-    s = enqueue_bp(r, a, 1, nullptr);
+    s = enqueue_bp(r, a, 1);
     if (s != MTR_OK) return s;
   }
   return MTR_OK;
@@ -262,13 +291,6 @@ bool concurrent_axes(const mtr_recon* r) {
   return r->K > 1 && !r->ctx->profiling && !(e && e[0] == '1');
 }
 
-// Restores the context stream when a fork/join section ends early.
-struct StreamRestore {
-  mtr_context* ctx;
-  cudaStream_t main;
-  ~StreamRestore() { ctx->stream = main; }
-};
-
 // MACE outer iterations [first, first + count): n_inner SIRT iterations of
 // every axis, then the MACE step.
 mtr_status enqueue_outer(mtr_recon* r, int first, int count) {
@@ -282,22 +304,13 @@ mtr_status enqueue_outer(mtr_recon* r, int first, int count) {
         if (s != MTR_OK) return s;
       }
     } else {
-      StreamRestore guard{ctx, ctx->stream};
-      cudaEvent_t fork = ctx->sync_event(0);
-      if (!fork) return set_error(ctx, MTR_ERR_CUDA, "event creation");
-      MTR_CK(ctx, cudaEventRecord(fork, guard.main));
-      for (int k = 0; k < K; ++k) {
-        cudaStream_t sk = ctx->side_stream(k);
-        cudaEvent_t join = ctx->sync_event(1 + k);
-        if (!sk || !join) return set_error(ctx, MTR_ERR_CUDA, "side stream creation");
-        MTR_CK(ctx, cudaStreamWaitEvent(sk, fork, 0));
-        ctx->stream = sk;
-        mtr_status s = enqueue_axis_chain(r, k, it);
-        if (s != MTR_OK) return s;
-        MTR_CK(ctx, cudaEventRecord(join, sk));
-        ctx->stream = guard.main;
-        MTR_CK(ctx, cudaStreamWaitEvent(guard.main, join, 0));
+      ForkJoin fj(ctx);  // every axis' chain on its own side stream, joined on any exit
+      mtr_status s = fj.fork(K);
+      for (int k = 0; s == MTR_OK && k < K; ++k) {
+        fj.use(k);
+        s = enqueue_axis_chain(r, k, it);
       }
+      if (s != MTR_OK) return s;
     }
     mtr_status st = recon_enqueue_mace(r, it);
     if (st != MTR_OK) return st;
@@ -337,8 +350,10 @@ mtr_status mtr::recon_enqueue_mace(mtr_recon* r, int it) {
   double* dch = r->dchange.as<double>();
   {
     ProfScope ps(ctx, MTR_KERNEL_MACE);
+    // the FP64 convergence sums cost five of the step's FP64 operations per
+    // voxel: only when a record is kept
     launch_mace(K, ws, xs, r->wavg.as<float>(), r->nv, r->p.mace_step, xcs, copy_kind_of(r->p.precision),
-                dch && it < r->p.iter_times ? dch + 2 * it : nullptr, ctx->stream);
+                r->record_changes && dch && it < r->p.iter_times ? dch + 2 * it : nullptr, ctx->stream);
   }
   MTR_CK_LAUNCH(ctx, "mace");
   return MTR_OK;
@@ -392,6 +407,7 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   r->p = *params;
   r->K = n_axes;
   r->nv = (long long)vol.X * vol.Y * vol.Z;
+  r->record_changes = (params->flags & MTR_FLAG_RECORD_CHANGES) != 0;
   r->ax.resize(n_axes);
   const bool mx = mixed(params->precision);
   const size_t vb = (size_t)r->nv * 4;
@@ -662,6 +678,8 @@ mtr_status mtr_recon_norms(mtr_recon* r, double* out, long long n) {
 
 mtr_status mtr_recon_changes(mtr_recon* r, double* out, int n) {
   if (!r || !out || n < 0) return MTR_ERR_INVALID_ARGUMENT;
+  if (!r->record_changes)
+    return set_error(r->ctx, MTR_ERR_INVALID_ARGUMENT, "convergence record not kept (MTR_FLAG_RECORD_CHANGES)");
   n = std::min(n, std::max(1, r->p.iter_times));
   DeviceGuard g(r->ctx->device);
   std::vector<double> raw(2 * (size_t)n);
@@ -675,6 +693,7 @@ mtr_status mtr_recon_changes(mtr_recon* r, double* out, int n) {
 mtr_status mtr_recon_run_until(mtr_recon* r, int first, double tol, int* outer_done) {
   if (!r || first < 0 || !(tol >= 0.0)) return MTR_ERR_INVALID_ARGUMENT;
   DeviceGuard g(r->ctx->device);
+  r->record_changes = true;  // the stopping rule reads the record
   int it = first;
   while (it < r->p.iter_times) {
     mtr_status s = enqueue_outer(r, it, 1);
@@ -730,7 +749,13 @@ mtr_status mtr_recon_destroy(mtr_recon* r) {
 
 mtr_status mtr_reconstruct(mtr_context* ctx, int n_axes, const mtr_axis* axes, mtr_volume_size vol,
                            const mtr_params* params, float* out_volume) {
-  if (!ctx || !out_volume) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "null argument");
+  if (!ctx || !out_volume || !axes) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "null argument");
+  if (n_axes <= 0 || n_axes > MTR_MAX_AXES) return set_error(ctx, MTR_ERR_INVALID_ARGUMENT, "axis count out of range");
+  // This entry point has no later upload: every axis must bring its projections.
+  for (int k = 0; k < n_axes; ++k) {
+    const mtr_status sa = check_axis(ctx, axes[k], true);
+    if (sa != MTR_OK) return sa;
+  }
   mtr_recon* r = nullptr;
   mtr_status s = mtr_recon_create(ctx, n_axes, axes, vol, params, MTR_MEM_HOST, &r);
   if (s != MTR_OK) return s;

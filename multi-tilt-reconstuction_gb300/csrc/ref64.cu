@@ -137,7 +137,8 @@ __global__ void mace64_kernel(int K, Mace64Ptrs P, double* __restrict__ wavg, lo
 
 unsigned grid_for(long long n) {
   long long b = (n + 255) / 256;
-  if (b > 152LL * 16) b = 152LL * 16;
+  const long long cap = (long long)device_sm_count() * 16;
+  if (b > cap) b = cap;
   return (unsigned)(b < 1 ? 1 : b);
 }
 

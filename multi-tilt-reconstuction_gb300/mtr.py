@@ -24,9 +24,10 @@ ERR_TIMEOUT, ERR_NOT_READY, ERR_CAPACITY = 8, 9, 10
 
 PREC_FP32, PREC_MIXED_BF16, PREC_MIXED_FP16 = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
-FLAG_RECORD_NORMS, FLAG_GRAPH, FLAG_HOST_VOLUMES = 1, 2, 4
+FLAG_RECORD_NORMS, FLAG_GRAPH, FLAG_HOST_VOLUMES, FLAG_RECORD_CHANGES = 1, 2, 4, 8
 MAX_AXES = 16
 KERNEL_CLASSES = ["wbp", "forward", "residual", "backproject", "mace", "other"]
+NOALLOC_SCRATCH_FLOATS = 8 * 1024 * 1024  # MTR_NOALLOC_SCRATCH_FLOATS
 
 
 class MtrError(RuntimeError):
@@ -121,6 +122,8 @@ _SIGNATURES = {
     "mtr_context_synchronize": (C.c_int, [_P]),
     "mtr_context_trim": (C.c_int, [_P]),
     "mtr_context_launch_count": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "mtr_context_windowed_launch_count": (C.c_int, [_P, C.POINTER(C.c_longlong)]),
+    "mtr_set_wait_limit": (C.c_int, [C.c_longlong]),
     "mtr_context_set_profiling": (C.c_int, [_P, C.c_int]),
     "mtr_context_profile": (C.c_int, [_P, C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_double)]),
     "mtr_context_profile_reset": (C.c_int, [_P]),
@@ -214,6 +217,23 @@ def _ptr(a) -> int:
     raise TypeError(f"unsupported buffer {type(a)}")
 
 
+def _numel(a) -> int:
+    return int(a.size) if isinstance(a, np.ndarray) else int(a.numel())
+
+
+def _require_half(a, what: str) -> None:
+    """FP16 entry points read 2 bytes per value: a buffer of any other type
+    would be reinterpreted silently."""
+    if isinstance(a, np.ndarray):
+        ok = a.dtype == np.float16
+    else:
+        import torch
+
+        ok = isinstance(a, torch.Tensor) and a.dtype == torch.float16
+    if not ok:
+        raise TypeError(f"{what}: needs IEEE FP16 data (numpy.float16 or torch.float16), got {getattr(a, 'dtype', type(a))}")
+
+
 @dataclass
 class AxisData:
     """One tilt axis: data [AngN, Y, X] float32 (numpy or CUDA tensor), coefficient arrays [AngN*4].
@@ -280,6 +300,12 @@ class Context:
     def launch_count(self) -> int:
         n = C.c_longlong()
         self.check(self.lib.mtr_context_launch_count(self.h, C.byref(n)), "launch_count")
+        return n.value
+
+    def windowed_launch_count(self) -> int:
+        """Launches of the TMA-windowed projector kernels issued so far."""
+        n = C.c_longlong()
+        self.check(self.lib.mtr_context_windowed_launch_count(self.h, C.byref(n)), "windowed_launch_count")
         return n.value
 
     def set_profiling(self, on: bool) -> None:
@@ -351,6 +377,7 @@ class Recon:
 
     def __init__(self, ctx: Context, axes: Sequence[AxisData], vol: VolumeSize, p: Params, mem_kind=MEM_HOST):
         self.ctx, self.vol, self.p, self.K = ctx, vol, p, len(axes)
+        self._shapes = [(a.prj.AngN, a.prj.Y, a.prj.X) for a in axes]
         arr = (AxisC * len(axes))(*[a.c_struct() for a in axes])
         h = _P()
         ctx.check(ctx.lib.mtr_recon_create(ctx.h, len(axes), arr, vol, C.byref(p), mem_kind, C.byref(h)),
@@ -362,6 +389,10 @@ class Recon:
 
     def upload_half(self, k: int, data, mem_kind=MEM_HOST) -> None:
         """Projections of axis k as IEEE FP16 (numpy float16 or a CUDA half tensor)."""
+        _require_half(data, "upload_half")
+        a, y, x = self._shapes[k]
+        if _numel(data) != a * y * x:
+            raise ValueError(f"upload_half: {_numel(data)} values given, axis {k} holds {a * y * x}")
         self.ctx.check(self.ctx.lib.mtr_recon_upload_half(self.h, k, _ptr(data), mem_kind), "mtr_recon_upload_half")
 
     def run(self) -> None:
@@ -566,8 +597,15 @@ def read_mrc_stack_device(ctx: "Context", path: str, out) -> None:
               "mtr_mrc_read_stack_device")
 
 
-def read_mrc_stack_device_half(ctx: "Context", path: str, out) -> None:
-    """Read an MRC stack's data into a CUDA float16 tensor `out`, rounded on the device."""
+def read_mrc_stack_device_half(ctx: "Context", path: str, out, n: int | None = None) -> None:
+    """Read an MRC stack's data into a CUDA float16 tensor `out`, rounded on the device.
+    n: values to read (default nx*ny*nz of the file); `out` must hold exactly n halves."""
+    _require_half(out, "read_mrc_stack_device_half")
+    if n is None:
+        h = read_mrc_header(path)
+        n = h.nx * h.ny * h.nz
+    if out.numel() != n:
+        raise ValueError(f"read_mrc_stack_device_half: tensor holds {out.numel()} halves, {n} requested")
     ctx.check(ctx.lib.mtr_mrc_read_stack_device_half(ctx.h, str(path).encode(), _ptr(out), out.numel()),
               "mtr_mrc_read_stack_device_half")
 

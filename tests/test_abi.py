@@ -101,3 +101,15 @@ def test_cli_help_and_bad_options():
     assert r.returncode != 0
     r = subprocess.run([str(cli), "-i", "2,a.st,a.txbr", "-o", "x.mrc"], capture_output=True, text=True)
     assert r.returncode != 0  # K=2 needs 4 paths
+
+
+def test_half_entry_points_reject_other_dtypes():
+    """The FP16 upload and reader read 2 bytes per value: any other dtype is
+    refused before the library sees it."""
+    import numpy as np
+
+    with pytest.raises(TypeError):
+        mtr._require_half(np.zeros(4, np.float32), "upload_half")
+    with pytest.raises(TypeError):
+        mtr._require_half(np.zeros(4, np.uint16), "upload_half")
+    mtr._require_half(np.zeros(4, np.float16), "upload_half")

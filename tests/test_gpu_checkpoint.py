@@ -83,7 +83,12 @@ def test_convergence_record_and_early_stop(ctx):
     iteration (FP64 on the GPU); mtr_recon_run_until stops on it."""
     c = cases.get("two_axis")
     p = mtr.params(iter_times=4, sirt_inner=3, sirt_step=0.5, mace_step=0.8)
-    r = mtr.Recon(ctx, c.axes, c.vol, p)
+    plain = mtr.Recon(ctx, c.axes, c.vol, p)  # no record kept unless asked for
+    with pytest.raises(mtr.MtrError):
+        plain.changes(4)
+    plain.close()
+    pr = mtr.params(iter_times=4, sirt_inner=3, sirt_step=0.5, mace_step=0.8, flags=mtr.FLAG_RECORD_CHANGES)
+    r = mtr.Recon(ctx, c.axes, c.vol, pr)
     r.init()
     vols = [r.download().astype(np.float64)]  # the WBP init consensus
     for it in range(4):

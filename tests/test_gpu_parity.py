@@ -222,3 +222,43 @@ def test_fp64_gpu_reference_matches_fp64_oracle(ctx, name):
     # near-zero-weight taps at the footprint edge (c == 0 vs c tiny); observed
     # ~1e-8, four to five orders below the errors this reference measures.
     assert rel_l2(got, want) < 1e-7
+
+
+def test_entry_points_without_projection_data_are_rejected(ctx):
+    """mtr_reconstruct and mtr_batch_create have no later upload, so an axis
+    without projection data is an invalid argument (mtr_recon_create alone
+    accepts it, for a later mtr_recon_upload)."""
+    import ctypes as C
+
+    c = cases.get("single")
+    shape_only = [mtr.AxisData(a.x_coef, a.y_coef, tuple(a.data.shape)) for a in c.axes]
+    arr = (mtr.AxisC * len(shape_only))(*[a.c_struct() for a in shape_only])
+    out = np.empty(c.vol.shape, np.float32)
+    p = mtr.params(iter_times=1, sirt_inner=1)
+    st = ctx.lib.mtr_reconstruct(ctx.h, len(shape_only), arr, c.vol, C.byref(p), out.ctypes.data)
+    assert st == mtr.ERR_INVALID_ARGUMENT
+    inst = (mtr.InstanceC * 1)(mtr.InstanceC(len(shape_only), arr, c.vol))
+    h = C.c_void_p()
+    st = ctx.lib.mtr_batch_create(ctx.h, 1, inst, C.byref(p), mtr.MEM_HOST, C.byref(h))
+    assert st == mtr.ERR_INVALID_ARGUMENT and not h.value
+    # the context still works
+    assert rel_l2(ctx.wbp(c.axes[0], c.vol), oracle.wbp(0, c.axes[0], c.vol)) < 1e-5
+
+
+@pytest.mark.parametrize("name", ["mid", "mid_oblique"])
+def test_reference_shaped_entry_points_run_windowed_kernels(ctx, name):
+    """mtr_wbp / mtr_sirt (the calls that replace ComputeInitialModel and
+    runSIRTOnGPU) run the TMA-windowed projectors where the windows fit, and
+    keep the oracle's result."""
+    c = cases.get(name)
+    a = c.axes[0]
+    n0 = ctx.windowed_launch_count()
+    x0 = ctx.wbp(a, c.vol)
+    n1 = ctx.windowed_launch_count()
+    got = ctx.sirt(a, c.vol, x0, n_inner=3, step=0.5)
+    n2 = ctx.windowed_launch_count()
+    assert n1 - n0 >= 1  # the WBP gather
+    assert n2 - n1 >= 1 + 2 * 3  # weight sums, then a forward splat and a back-projection per iteration
+    assert rel_l2(x0, oracle.wbp(oracle.REF_FAITHFUL, a, c.vol)) < 1e-5
+    want = oracle.sirt(oracle.REF_FAITHFUL, a, c.vol, x0, 3, 0.5)
+    assert rel_l2(got, want) < FP32_TOL
