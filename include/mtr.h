@@ -21,7 +21,7 @@
 extern "C" {
 #endif
 
-#define MTR_ABI_VERSION 1
+#define MTR_ABI_VERSION 2
 /* Maximum tilt axes per reconstruction (MAX_TILT, ReadAndInitialOptions.h:17). */
 #define MTR_MAX_AXES 16
 /* Default SIRT iterations per MACE iteration (hard-coded, FunctionOnGPU.cu:212). */
@@ -85,6 +85,7 @@ typedef struct mtr_params {
   float mace_step;  /* -m: MACE Mann step rho (default 0.7) */
   int precision;    /* mtr_precision */
   int flags;        /* MTR_FLAG_* */
+  int slab_depth;   /* Z planes per streamed slab (MTR_FLAG_STREAM_SLABS); 0 = automatic (32) */
 } mtr_params;
 
 /* Record the squared residual norm (FP64) of every SIRT iteration. */
@@ -102,6 +103,18 @@ typedef struct mtr_params {
  * relative change of the consensus per outer iteration, two FP64 sums per
  * voxel in the MACE step.  mtr_recon_run_until turns it on by itself. */
 #define MTR_FLAG_RECORD_CHANGES 8
+/* Single-GPU streaming slab loop: the volume-sized arrays (iterates, MACE
+ * states, weight sums, forward copies, consensus) live in pinned host memory,
+ * and the device holds the projection-space arrays plus a working set of two
+ * Z-slabs of slab_depth planes.  Each SIRT iteration of an axis splats the
+ * slabs one after another into the axis' ray sums, forms the residual once
+ * after the last slab, then back-projects the slabs one after another, each
+ * slab's copies overlapping the other slab's kernels.  Replaces the
+ * reference's Z-slab decomposition over MPI ranks (divideSlice,
+ * MultiAxis.cpp:13-31), whose partial ray sums are reduced in projection
+ * space every SIRT iteration (FunctionOnGPU.cu:218-238).  The axes run one
+ * after another; MTR_FLAG_GRAPH is ignored. */
+#define MTR_FLAG_STREAM_SLABS 16
 
 /* Fill p with the reference defaults (Options(), ReadAndInitialOptions.h:33-42). */
 void mtr_params_default(mtr_params* p);

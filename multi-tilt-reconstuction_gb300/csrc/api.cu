@@ -65,6 +65,7 @@ void mtr_params_default(mtr_params* p) {
   p->mace_step = 0.7f;
   p->precision = MTR_PREC_FP32;
   p->flags = 0;
+  p->slab_depth = 0;
 }
 
 mtr_status mtr_context_create(int device, mtr_context** out) {

@@ -5,6 +5,7 @@
 #include <atomic>
 #include <cstdint>
 #include <cstdlib>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -304,8 +305,40 @@ bool tma_disabled();
 // the forward splat for one axis, timing candidates on the axis' buffers
 // before they hold data, and encodes the tensor maps.
 bool autotune_enabled();
+// Candidates run over the frame v on device scratch: scratch_vol / scratch_cbp
+// (FP32) and, in mixed precision, scratch_copy (the BF16 / FP16 copy the
+// forward splat reads); none of them holds data yet.
 bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, float* scratch_vol,
-               float* scratch_cbp, int* err);
+               float* scratch_cbp, void* scratch_copy, int* err);
+
+// The Z planes [z0, z1) one launch works on and the arrays that hold exactly
+// those planes: an axis' whole volume arrays, or one slot of a streamed
+// reconstruction's device working set.
+struct VolSpan {
+  int z0, z1;
+  float* x;     // SIRT iterate (the WBP writes it)
+  float* cbp;   // back-projection weight sums
+  void* xcopy;  // BF16 / FP16 copy of x read by the forward splat (mixed), or null
+};
+
+// Device working set of a reconstruction whose volume-sized arrays live in
+// host memory (MTR_FLAG_STREAM_SLABS, stream.cu).  The volume is cut into
+// Z-slabs of `depth` planes; two slab slots rotate so that the copy of one
+// slab overlaps the kernels of the other.  `in` carries host-to-device
+// copies, `out` device-to-host copies, the context stream the kernels.
+struct SlabStream {
+  int depth = 0;           // Z planes per slab
+  int nslab = 0;
+  long long plane = 0;     // voxels per Z plane
+  int mace_planes = 0;     // Z planes per MACE chunk
+  DevBuf x[2], cbp[2], xc[2];  // slot arrays (x/cbp FP32, xc the forward copy in mixed precision)
+  DevBuf acc;              // one slab of the WBP sum over axes (initialisation)
+  DevBuf mace;             // one MACE chunk: w_k, x_k (FP32), w_avg, then the K forward copies
+  cudaStream_t in = nullptr, out = nullptr;
+  cudaEvent_t loaded[2] = {}, computed[2] = {}, freed[2] = {}, mark[3] = {};
+  long long device_bytes = 0;
+  ~SlabStream();
+};
 
 }  // namespace mtr
 
@@ -361,5 +394,31 @@ struct mtr_recon {
   int outer_done = 0;           // MACE outer iterations the state has been through
   cudaGraphExec_t graph = nullptr;
   long long graph_nodes = 0;
+  // Streamed slabs (MTR_FLAG_STREAM_SLABS): the volume-sized arrays above are
+  // in pinned, mapped host memory and this is the device working set.
+  std::unique_ptr<mtr::SlabStream> slabs;
   ~mtr_recon();
 };
+
+namespace mtr {
+// Pieces of a reconstruction's schedule over one span of axis k's volume (recon.cu).
+mtr_status recon_enqueue_forward_span(mtr_recon* r, int k, const VolSpan& sp);
+// mode 0 WBP, 1 SIRT update; widen: widen FP16 projections for a windowed WBP first.
+mtr_status recon_enqueue_bp_span(mtr_recon* r, int k, int mode, const VolSpan& sp, bool widen);
+mtr_status recon_enqueue_widen(mtr_recon* r, int k);
+// Residual of axis k; norm: FP64 sum of r^2 (null: not recorded).
+mtr_status recon_enqueue_residual_norm(mtr_recon* r, int k, double* norm);
+// Where the squared residual norm of (outer it, axis k, inner j) is recorded, or null.
+double* recon_norm_slot(mtr_recon* r, int it, int k, int j);
+// The MACE step's FP64 convergence sums of outer iteration it, or null.
+double* recon_change_slot(mtr_recon* r, int it);
+int recon_copy_kind(const mtr_recon* r);
+// Streamed slabs (stream.cu): the device working set, the WBP initialisation
+// and the MACE outer iterations with slabs streamed through it.
+mtr_status stream_setup(mtr_recon* r);
+mtr_status stream_enqueue_init(mtr_recon* r);
+mtr_status stream_enqueue_outer(mtr_recon* r, int first, int count);
+// The copy streams wait for the work enqueued so far on the context stream
+// (after the context stream wrote the host-side volume arrays itself).
+mtr_status stream_join(mtr_recon* r);
+}  // namespace mtr

@@ -115,16 +115,6 @@ mtr_status enqueue_geometry(mtr_recon* r) {
   return MTR_OK;
 }
 
-// The Z planes [z0, z1) one launch works on and the arrays that hold exactly
-// those planes: an axis' whole device arrays, or one slot of a streamed
-// reconstruction's device working set.
-struct VolSpan {
-  int z0, z1;
-  float* x;     // SIRT iterate (the WBP writes it)
-  float* cbp;   // back-projection weight sums
-  void* xcopy;  // BF16 / FP16 copy of x read by the forward splat (mixed), or null
-};
-
 VolSpan whole_volume(const mtr_recon* r, AxisState& a) {
   return VolSpan{r->vol.Zs, r->vol.Zs + r->vol.NZ, a.x.as<float>(), a.cbp.as<float>(), a.xcopy.p};
 }
@@ -226,6 +216,7 @@ mtr_status enqueue_bp(mtr_recon* r, AxisState& a, int mode) { return enqueue_bp(
 // WBP init: w_avg = sum of per-axis WBPs, w_k = z_k = w_avg (and the
 // forward-read copies), norms and change records reset.
 mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
+  if (r->slabs) return stream_enqueue_init(r);
   mtr_context* ctx = r->ctx;
   const long long nv = r->nv;
   const size_t vbytes = (size_t)nv * 4;
@@ -259,6 +250,26 @@ mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
   return MTR_OK;
 }
 
+mtr_status mtr::recon_enqueue_forward_span(mtr_recon* r, int k, const VolSpan& sp) {
+  return enqueue_forward(r, r->ax[k], sp);
+}
+mtr_status mtr::recon_enqueue_bp_span(mtr_recon* r, int k, int mode, const VolSpan& sp, bool widen) {
+  return enqueue_bp(r, r->ax[k], mode, sp, widen);
+}
+mtr_status mtr::recon_enqueue_widen(mtr_recon* r, int k) { return enqueue_widen_for_wbp(r, r->ax[k]); }
+mtr_status mtr::recon_enqueue_residual_norm(mtr_recon* r, int k, double* norm) {
+  return enqueue_residual(r, r->ax[k], norm);
+}
+double* mtr::recon_norm_slot(mtr_recon* r, int it, int k, int j) {
+  double* norms = r->norms.as<double>();
+  if (!norms || it >= r->p.iter_times) return nullptr;
+  return norms + ((long long)it * r->K + k) * r->p.sirt_inner + j;
+}
+double* mtr::recon_change_slot(mtr_recon* r, int it) {
+  double* dch = r->dchange.as<double>();
+  return r->record_changes && dch && it < r->p.iter_times ? dch + 2 * it : nullptr;
+}
+int mtr::recon_copy_kind(const mtr_recon* r) { return copy_kind_of(r->p.precision); }
 mtr_status mtr::recon_enqueue_wbp(mtr_recon* r, int k) { return enqueue_bp(r, r->ax[k], 0); }
 mtr_status mtr::recon_enqueue_forward(mtr_recon* r, int k) { return enqueue_forward(r, r->ax[k]); }
 mtr_status mtr::recon_enqueue_residual(mtr_recon* r, int k) { return enqueue_residual(r, r->ax[k], nullptr); }
@@ -294,6 +305,7 @@ bool concurrent_axes(const mtr_recon* r) {
 // MACE outer iterations [first, first + count): n_inner SIRT iterations of
 // every axis, then the MACE step.
 mtr_status enqueue_outer(mtr_recon* r, int first, int count) {
+  if (r->slabs) return stream_enqueue_outer(r, first, count);
   mtr_context* ctx = r->ctx;
   const int K = r->K;
   const bool par = concurrent_axes(r);
@@ -412,9 +424,16 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
   const bool mx = mixed(params->precision);
   const size_t vb = (size_t)r->nv * 4;
   // volume arrays in mapped host memory (MTR_FLAG_HOST_VOLUMES) or in HBM
-  const bool hv = (params->flags & MTR_FLAG_HOST_VOLUMES) != 0;
+  // (streamed slabs keep them in host memory too, and a device working set)
+  const bool streamed = (params->flags & MTR_FLAG_STREAM_SLABS) != 0;
+  const bool hv = streamed || (params->flags & MTR_FLAG_HOST_VOLUMES) != 0;
   MTR_CK(ctx, r->wavg.alloc_where(vb, hv, ctx));
   MTR_CK(ctx, r->err.alloc_pooled(sizeof(int), ctx));
+  if (streamed) {
+    s = stream_setup(r.get());
+    if (s != MTR_OK) return s;
+    r->bytes += r->slabs->device_bytes;
+  }
   MTR_CK(ctx, cudaMemsetAsync(r->err.p, 0, sizeof(int), ctx->stream));
   r->bytes += hv ? 0 : vb;
   for (int k = 0; k < n_axes; ++k) {
@@ -453,7 +472,15 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
       // WBP over b; with FP16 projections over their FP32 widening in r (r is
       // free until the first residual), so the WBP gathers FP32 like SIRT.
       // SIRT back-projection over the FP32 residual and the forward splat: tuned depths
-      tune_axis(ctx, a, r->vol, params->precision, a.w.as<float>(), a.cbp.as<float>(), r->err.as<int>());
+      if (streamed) {  // candidates over one slab, in the slot arrays the run uses
+        VolDev tv = r->vol;
+        tv.NZ = r->slabs->depth;
+        tune_axis(ctx, a, tv, params->precision, r->slabs->x[0].as<float>(), r->slabs->cbp[0].as<float>(),
+                  r->slabs->xc[0].p, r->err.as<int>());
+      } else {
+        tune_axis(ctx, a, r->vol, params->precision, a.w.as<float>(), a.cbp.as<float>(), a.xcopy.p,
+                  r->err.as<int>());
+      }
       // The WBP gathers the same windows as the SIRT update: the lane layout
       // tuned for it (lines or 8x4 patches), at depth 16 where the tuned depth
       // is 16 or more, else 8.
@@ -591,7 +618,8 @@ mtr_status mtr_recon_load(mtr_recon* r, const char* path, int* outer_done) {
   }
   r->outer_done = h.outer_done;
   if (outer_done) *outer_done = h.outer_done;
-  return MTR_OK;
+  // a streamed run copies these host arrays in on its own streams
+  return r->slabs ? stream_join(r) : MTR_OK;
 }
 
 mtr_status mtr_recon_run(mtr_recon* r) {
@@ -599,7 +627,8 @@ mtr_status mtr_recon_run(mtr_recon* r) {
   mtr_context* ctx = r->ctx;
   DeviceGuard g(ctx->device);
   r->outer_done = r->p.iter_times;
-  if (!(r->p.flags & MTR_FLAG_GRAPH)) return enqueue_run(r);
+  // (a streamed run waits on copies between its streams: not captured)
+  if (!(r->p.flags & MTR_FLAG_GRAPH) || r->slabs) return enqueue_run(r);
   if (!r->graph) {
     cudaGraph_t graph = nullptr;
     MTR_CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));

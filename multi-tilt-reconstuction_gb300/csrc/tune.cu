@@ -151,7 +151,7 @@ bool autotune_enabled() {
 // Chooses a.plan (SIRT back-projection over r) and a.fplan (forward splat
 // over s) for one axis and encodes the matching tensor maps.  Leaves s zeroed.
 bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, float* scratch_vol,
-               float* scratch_cbp, int* err) {
+               float* scratch_cbp, void* scratch_copy, int* err) {
   const int copy_kind = precision == MTR_PREC_MIXED_BF16 ? 1 : precision == MTR_PREC_MIXED_FP16 ? 2 : 0;
   const std::string key = geometry_key(a, v, precision);
   Choice ch;
@@ -198,7 +198,7 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
         const BpPlan* pp = &bps.back();
         const CUtensorMap* mp = &bmaps.back();
         cands.push_back([=, &a, &v] {
-          return launch_backproject_tma<float>(*mp, *pp, a.dev(), v, 1, 0.5f, scratch_vol, scratch_cbp, a.xcopy.p,
+          return launch_backproject_tma<float>(*mp, *pp, a.dev(), v, 1, 0.5f, scratch_vol, scratch_cbp, scratch_copy,
                                                copy_kind, z0, z1, err, ctx->stream);
         });
         what.push_back({nz, lane});
@@ -227,11 +227,13 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
         const CUtensorMap* mp = &fmaps.back();
         cands.push_back([=, &a, &v] {
           if (copy_kind == 1)
-            return launch_forward_tma<__nv_bfloat16>(*mp, *pp, a.dev(), v, a.xcopy.as<__nv_bfloat16>(), z0, z1, err,
+            return launch_forward_tma<__nv_bfloat16>(*mp, *pp, a.dev(), v,
+                                                     static_cast<const __nv_bfloat16*>(scratch_copy), z0, z1, err,
                                                      ctx->stream);
           if (copy_kind == 2)
-            return launch_forward_tma<__half>(*mp, *pp, a.dev(), v, a.xcopy.as<__half>(), z0, z1, err, ctx->stream);
-          return launch_forward_tma<float>(*mp, *pp, a.dev(), v, a.x.as<float>(), z0, z1, err, ctx->stream);
+            return launch_forward_tma<__half>(*mp, *pp, a.dev(), v, static_cast<const __half*>(scratch_copy), z0, z1,
+                                              err, ctx->stream);
+          return launch_forward_tma<float>(*mp, *pp, a.dev(), v, scratch_vol, z0, z1, err, ctx->stream);
         });
         what.push_back({nz, lane});
       }

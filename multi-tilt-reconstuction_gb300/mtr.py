@@ -24,7 +24,7 @@ ERR_TIMEOUT, ERR_NOT_READY, ERR_CAPACITY = 8, 9, 10
 
 PREC_FP32, PREC_MIXED_BF16, PREC_MIXED_FP16 = 0, 1, 2
 MEM_HOST, MEM_DEVICE = 0, 1
-FLAG_RECORD_NORMS, FLAG_GRAPH, FLAG_HOST_VOLUMES, FLAG_RECORD_CHANGES = 1, 2, 4, 8
+FLAG_RECORD_NORMS, FLAG_GRAPH, FLAG_HOST_VOLUMES, FLAG_RECORD_CHANGES, FLAG_STREAM_SLABS = 1, 2, 4, 8, 16
 MAX_AXES = 16
 KERNEL_CLASSES = ["wbp", "forward", "residual", "backproject", "mace", "other"]
 NOALLOC_SCRATCH_FLOATS = 8 * 1024 * 1024  # MTR_NOALLOC_SCRATCH_FLOATS
@@ -83,7 +83,7 @@ class ServerStats(C.Structure):
 
 class Params(C.Structure):
     _fields_ = [("iter_times", C.c_int), ("sirt_inner", C.c_int), ("sirt_step", C.c_float),
-                ("mace_step", C.c_float), ("precision", C.c_int), ("flags", C.c_int)]
+                ("mace_step", C.c_float), ("precision", C.c_int), ("flags", C.c_int), ("slab_depth", C.c_int)]
 
 
 class MrcHeader(C.Structure):
@@ -258,8 +258,9 @@ class AxisData:
         return AxisC(self.prj, self.x_coef.ctypes.data_as(dp), self.y_coef.ctypes.data_as(dp), ptr)
 
 
-def params(iter_times=5, sirt_inner=10, sirt_step=0.5, mace_step=0.7, precision=PREC_FP32, flags=0) -> Params:
-    return Params(iter_times, sirt_inner, sirt_step, mace_step, precision, flags)
+def params(iter_times=5, sirt_inner=10, sirt_step=0.5, mace_step=0.7, precision=PREC_FP32, flags=0,
+           slab_depth=0) -> Params:
+    return Params(iter_times, sirt_inner, sirt_step, mace_step, precision, flags, slab_depth)
 
 
 class Context:

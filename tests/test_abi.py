@@ -40,7 +40,7 @@ def test_binding_covers_header():
 
 def test_abi_version_and_status_strings():
     lib = mtr.load()
-    assert lib.mtr_abi_version() == 1
+    assert lib.mtr_abi_version() == 2
     assert lib.mtr_status_string(0) == b"ok"
     assert lib.mtr_status_string(3) == b"out of device memory"
     assert lib.mtr_status_string(999) == b"unknown status"
