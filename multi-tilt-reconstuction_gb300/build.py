@@ -28,7 +28,7 @@ NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-Wall", "-Wno-unused-function", "-I", str(INCLUDE)]
 
 CU_SOURCES = ["projector.cu", "bp_tma.cu", "fwd_tma.cu", "mace.cu", "api.cu", "recon.cu", "entry.cu", "ref64.cu",
-              "noalloc.cu", "tune.cu", "batch.cu", "serve.cu", "mrc_device.cu", "stream.cu"]
+              "noalloc.cu", "tune.cu", "batch.cu", "serve.cu", "mrc_device.cu", "stream.cu", "bp_pairs.cu"]
 CXX_SOURCES = ["mrc_io.cpp", "options.cpp", "geometry.cpp"]
 
 
@@ -40,7 +40,7 @@ def nvcc() -> str:
 
 
 def _headers() -> list[Path]:
-    return list(CSRC.glob("*.h")) + list(INCLUDE.glob("*.h"))
+    return list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
 
 
 def _stale(target: Path, deps: list[Path]) -> bool:

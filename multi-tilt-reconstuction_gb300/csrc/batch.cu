@@ -98,8 +98,9 @@ mtr_status mtr::build_sirt_tables(mtr_context* ctx, const std::vector<mtr_recon*
       const int bgy = (v.NY + (bp.lanes == 1 ? 32 : 8) - 1) / (bp.lanes == 1 ? 32 : 8);
       const int fgx = (v.NX + (fp.lanes == 1 ? 8 : 32) - 1) / (fp.lanes == 1 ? 8 : 32);
       const int fgy = (v.NY + (fp.lanes == 1 ? 32 : 8) - 1) / (fp.lanes == 1 ? 32 : 8);
-      // the persistent kernels take lines along X or Y, depths up to 16, of small axes
-      const bool bp_ok = a.tma && !tma_disabled() && bp.lanes != 2 && bp.nz <= 16 &&
+      // the persistent kernels take lines along X or Y over FP32 windows,
+      // depths up to 16, of small axes
+      const bool bp_ok = a.tma && !tma_disabled() && bp.lanes != 2 && !bp.pairs && bp.nz <= 16 &&
                          (long long)bgx * bgy * ((v.NZ + bp.nz - 1) / bp.nz) <
                              (long long)kOwnWaves * ctx->num_sms * backproject_batch_ctas_per_sm(bp.smem);
       const bool fwd_ok = a.ftma && !tma_disabled() && fp.lanes != 2 &&

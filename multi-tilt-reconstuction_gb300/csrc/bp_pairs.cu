@@ -1,0 +1,26 @@
+// The SIRT back-projection update over windows of residual pairs.
+//
+// The residual of such an axis is written as (value, next value - value)
+// pairs, one per detector pixel (residual_pairs_kernel), so a voxel's two
+// taps of one detector row are one 8-byte shared-memory load and their x
+// interpolation one FFMA (the FP32-window kernel needs two loads, a
+// subtraction and an FFMA).  Twice the window bytes: the tuner keeps this
+// layout for an axis only where it measures faster (on lines of lanes that
+// share detector rows it saves a third of the instructions; on oblique axes
+// the 8-byte loads of a warp conflict in the shared-memory banks).  Separate
+// from bp_tma.cu so that the two sets of instantiations compile in parallel.
+#include "bp_brick.cuh"
+
+namespace mtr {
+
+cudaError_t launch_backproject_tma_pairs(const CUtensorMap& map, const BpPlan& plan, const BpArgs& P,
+                                         cudaStream_t st) {
+  if (plan.lanes == 2) return plan.bz0 ? launch_nz<float, 1, true, 2, true>(map, P, plan, st)
+                                       : launch_nz<float, 1, true, 2, false>(map, P, plan, st);
+  if (plan.lanes == 1) return plan.bz0 ? launch_nz<float, 1, true, 1, true>(map, P, plan, st)
+                                       : launch_nz<float, 1, true, 1, false>(map, P, plan, st);
+  return plan.bz0 ? launch_nz<float, 1, true, 0, true>(map, P, plan, st)
+                  : launch_nz<float, 1, true, 0, false>(map, P, plan, st);
+}
+
+}  // namespace mtr

@@ -276,6 +276,7 @@ struct DevBuf {
 struct AxisState {
   int PX = 0, PY = 0, A = 0;
   int pitch = 0;          // row pitch of projection-space arrays (elements)
+  int pitch2 = 0;         // row pitch of the residual in pair form (pairs, pair_pitch(PX))
   long long np = 0;       // A*PY*pitch
   std::vector<double> hxc, hyc;  // host copies of the maps (kernel planning)
   BpPlan plan;            // TMA back-projection window plan over r (FP32)
@@ -289,13 +290,26 @@ struct AxisState {
   DevBuf b;               // projections: float (FP32) or half (mixed)
   DevBuf s;               // forward accumulator, float
   DevBuf cf;              // forward row sums A 1, float
-  DevBuf r;               // residual, float
+  DevBuf r;               // residual: FP32 [A][PY][pitch], or pairs [A][PY][pitch2] when the
+                          // windowed back-projection reads it (tma)
   DevBuf cbp;             // back-projection weight sums A^T 1 (volume), float
   DevBuf w;               // MACE state w_k (volume), float
   DevBuf x;               // SIRT iterate z_k -> v_k (volume), float
   DevBuf xcopy;           // bf16/f16 copy of x read by the forward pass (mixed)
   AxisDev dev() const { return AxisDev{PX, PY, A, xc.as<double>(), yc.as<double>(), pitch}; }
 };
+
+// Tensor map over an axis' residual in pair form: FP32 elements, rows of
+// 2 * pitch2 floats, boxes of 2 * WX floats (WX pairs) by WY rows.
+inline bool encode_pair_map(CUtensorMap* m, const AxisState& a, const BpPlan& p) {
+  return p.pairs && encode_tensor_map_3d(m, a.r.p, false, 2 * a.pitch2, 2 * a.pitch2, a.PY, a.A, 2 * p.WX, p.WY);
+}
+// Tensor map over an axis' residual in the form its SIRT update reads: pairs,
+// or FP32 rows of `pitch` elements.
+inline bool encode_residual_map(CUtensorMap* m, const AxisState& a, const BpPlan& p) {
+  return p.pairs ? encode_pair_map(m, a, p)
+                 : encode_tensor_map_3d(m, a.r.p, false, a.PX, a.pitch, a.PY, a.A, p.WX, p.WY);
+}
 
 // Disable the TMA kernels (MTR_DISABLE_TMA=1 in the environment) to run the
 // plain global-memory kernels instead; used to cross-check the two paths.

@@ -276,6 +276,72 @@ residual_kernel(long long n, long long n4, const BT* __restrict__ b, float* __re
   }
 }
 
+// Residual of one detector row in pair form, for the windowed SIRT update:
+// pair column c = (r[c-1], r[c] - r[c-1]), r[-1] = 0 and r = 0 at and beyond
+// the detector's right edge (the zero padding of b, s and c gives r = 0 there
+// by itself); a back-projection tap at pixel ix reads pair column ix + 1.  The
+// calling warp's lane l takes columns [c0 + 4l, c0 + 4l + 4) of each 128-column
+// chunk; r[c-1] of a lane's first column comes from the lane below (lane 0:
+// the last column of the previous chunk).  s is reset to zero.  Returns the
+// lane's sum of r^2.
+template <typename BT>
+__device__ __forceinline__ float residual_pair_row(const BT* __restrict__ br, float* __restrict__ sr,
+                                                   const float* __restrict__ cr, float2* __restrict__ out, int pitch,
+                                                   int pitch2, int lane) {
+  float carry = 0.f, sq = 0.f;
+  for (int c0 = 0; c0 < pitch2; c0 += 128) {
+    const int col = c0 + 4 * lane;
+    float r4[4] = {0.f, 0.f, 0.f, 0.f};
+    if (col < pitch) {  // pitch is a multiple of 8: the four columns are all in the row
+      float bv[4];
+      ld4(br + col, bv);
+      const float4 sv = *reinterpret_cast<const float4*>(sr + col);
+      const float4 cv = __ldg(reinterpret_cast<const float4*>(cr + col));
+      r4[0] = bv[0] - (cv.x != 0.f ? sv.x / cv.x : sv.x);
+      r4[1] = bv[1] - (cv.y != 0.f ? sv.y / cv.y : sv.y);
+      r4[2] = bv[2] - (cv.z != 0.f ? sv.z / cv.z : sv.z);
+      r4[3] = bv[3] - (cv.w != 0.f ? sv.w / cv.w : sv.w);
+      *reinterpret_cast<float4*>(sr + col) = make_float4(0.f, 0.f, 0.f, 0.f);
+      sq += r4[0] * r4[0] + r4[1] * r4[1] + r4[2] * r4[2] + r4[3] * r4[3];
+    }
+    float prev = __shfl_up_sync(0xffffffffu, r4[3], 1);
+    if (lane == 0) prev = carry;
+    carry = __shfl_sync(0xffffffffu, r4[3], 31);
+    if (col < pitch2) {  // pitch2 is a multiple of 4: four pairs, 32 bytes
+      float4* o = reinterpret_cast<float4*>(out + col);
+      o[0] = make_float4(prev, r4[0] - prev, r4[0], r4[1] - r4[0]);
+      o[1] = make_float4(r4[1], r4[2] - r4[1], r4[2], r4[3] - r4[2]);
+    }
+  }
+  return sq;
+}
+
+// One warp per detector row (rows = AngN * PY); FP64 norm when NORM.
+template <typename BT, bool NORM>
+__global__ void __launch_bounds__(256)
+residual_pairs_kernel(long long rows, int pitch, int pitch2, const BT* __restrict__ b, float* __restrict__ s,
+                      const float* __restrict__ c, float2* __restrict__ rp, double* __restrict__ norm2) {
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  double acc = 0.0;
+  for (long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; row < rows; row += nwarps) {
+    const float sq = residual_pair_row(b + row * pitch, s + row * pitch, c + row * pitch, rp + row * pitch2, pitch,
+                                       pitch2, lane);
+    if (NORM) acc += (double)sq;
+  }
+  if (NORM) {
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ double red[8];
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+      atomicAdd(norm2, t);
+    }
+  }
+}
+
 // Residual over many axes: item = (descriptor, chunk of kBatchChunk pixels).
 template <bool HALF_B>
 __global__ void __launch_bounds__(256)
@@ -340,6 +406,22 @@ void launch_residual_batch(const ResBatchDesc* descs, const long long* first, in
   if (half_b) residual_batch_kernel<true><<<grid, 256, 0, st>>>(descs, first, n_desc, n_items);
   else residual_batch_kernel<false><<<grid, 256, 0, st>>>(descs, first, n_desc, n_items);
 }
+
+template <typename BT>
+void launch_residual_pairs(long long rows, int pitch, int pitch2, const BT* b, float* s, const float* c, float2* rp,
+                           double* norm2, cudaStream_t st) {
+  long long blocks = (rows + 7) / 8;  // 8 warps per block, one row per warp
+  const long long cap = (long long)device_sm_count() * 16;
+  if (blocks > cap) blocks = cap;  // grid-stride over the rest
+  if (blocks < 1) blocks = 1;
+  if (norm2) residual_pairs_kernel<BT, true><<<(unsigned)blocks, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
+  else residual_pairs_kernel<BT, false><<<(unsigned)blocks, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
+}
+
+template void launch_residual_pairs<float>(long long, int, int, const float*, float*, const float*, float2*, double*,
+                                           cudaStream_t);
+template void launch_residual_pairs<__half>(long long, int, int, const __half*, float*, const float*, float2*,
+                                            double*, cudaStream_t);
 
 template void launch_backproject<float>(const AxisDev&, const VolDev&, const float*, int, float, float*, float*,
                                         void*, int, int, int, cudaStream_t);

@@ -38,13 +38,20 @@ int copy_kind_of(int precision) {
 
 bool mixed(int precision) { return precision != MTR_PREC_FP32; }
 
-long long axis_bytes(long long np, long long nv, int precision) {
+// Bytes of the residual array of an axis: room for the FP32 residual and for
+// its pair form (8 bytes per pixel plus one column), whichever the axis' back-
+// projection reads.
+long long residual_bytes(int PX, int PY, int A) {
+  return std::max((long long)projection_pitch(PX) * PY * A * 4, (long long)pair_pitch(PX) * PY * A * 8);
+}
+
+long long axis_bytes(long long np, long long r_bytes, long long nv, int precision) {
   const long long pe = mixed(precision) ? 2 : 4;
   long long b = 0;
   b += np * pe;       // b
   b += np * 4;        // s
   b += np * 4;        // cf
-  b += np * 4;        // r (FP32 in every mode: the back-projection reads it per tap)
+  b += r_bytes;       // r (FP32 values in every mode: the back-projection reads them per tap)
   b += nv * 4 * 3;    // cbp, w, x
   if (mixed(precision)) b += nv * 2;  // xcopy
   return b;
@@ -154,12 +161,21 @@ mtr_status enqueue_forward(mtr_recon* r, AxisState& a) { return enqueue_forward(
 mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
   mtr_context* ctx = r->ctx;
   ProfScope ps(ctx, MTR_KERNEL_RESIDUAL);
-  if (mixed(r->p.precision))
+  const long long rows = (long long)a.A * a.PY;
+  if (a.tma && a.plan.pairs) {  // this axis' windowed update reads (value, next - value) pairs
+    if (mixed(r->p.precision))
+      launch_residual_pairs<__half>(rows, a.pitch, a.pitch2, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(),
+                                    a.r.as<float2>(), norm, ctx->stream);
+    else
+      launch_residual_pairs<float>(rows, a.pitch, a.pitch2, a.b.as<float>(), a.s.as<float>(), a.cf.as<float>(),
+                                   a.r.as<float2>(), norm, ctx->stream);
+  } else if (mixed(r->p.precision)) {
     launch_residual<__half, float>(a.np, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), norm,
                                    ctx->stream);
-  else
+  } else {
     launch_residual<float, float>(a.np, a.b.as<float>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), norm,
                                   ctx->stream);
+  }
   MTR_CK_LAUNCH(ctx, "residual");
   return MTR_OK;
 }
@@ -380,7 +396,7 @@ mtr_status mtr_estimate_footprint(int n_axes, const mtr_projection_size* prjs, m
   long long b = nv * 4;  // wavg
   for (int k = 0; k < n_axes; ++k) {
     const long long np = (long long)projection_pitch(prjs[k].X) * prjs[k].Y * prjs[k].AngN;
-    b += axis_bytes(np, nv, precision) + 64LL * prjs[k].AngN;
+    b += axis_bytes(np, residual_bytes(prjs[k].X, prjs[k].Y, prjs[k].AngN), nv, precision) + 64LL * prjs[k].AngN;
   }
   *bytes = b;
   return MTR_OK;
@@ -451,16 +467,18 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     MTR_CK(ctx, a.b.alloc_pooled((size_t)a.np * pe, ctx));
     MTR_CK(ctx, a.s.alloc_pooled((size_t)a.np * 4, ctx));
     MTR_CK(ctx, a.cf.alloc_pooled((size_t)a.np * 4, ctx));
-    MTR_CK(ctx, a.r.alloc_pooled((size_t)a.np * 4, ctx));
+    a.pitch2 = pair_pitch(a.PX);
+    const long long rb = residual_bytes(a.PX, a.PY, a.A);
+    MTR_CK(ctx, a.r.alloc_pooled((size_t)rb, ctx));
     MTR_CK(ctx, a.cbp.alloc_where(vb, hv, ctx));
     MTR_CK(ctx, a.w.alloc_where(vb, hv, ctx));
     MTR_CK(ctx, a.x.alloc_where(vb, hv, ctx));
     if (mx) MTR_CK(ctx, a.xcopy.alloc_where((size_t)r->nv * 2, hv, ctx));
-    r->bytes += axis_bytes(a.np, hv ? 0 : r->nv, params->precision) + 64LL * a.A;  // device bytes
+    r->bytes += axis_bytes(a.np, rb, hv ? 0 : r->nv, params->precision) + 64LL * a.A;  // device bytes
     MTR_CK(ctx, cudaMemcpyAsync(a.xc.p, axes[k].x_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemcpyAsync(a.yc.p, axes[k].y_coef, sizeof(double) * 4 * a.A, cudaMemcpyHostToDevice, ctx->stream));
     MTR_CK(ctx, cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream));
-    MTR_CK(ctx, cudaMemsetAsync(a.r.p, 0, (size_t)a.np * 4, ctx->stream));
+    MTR_CK(ctx, cudaMemsetAsync(a.r.p, 0, (size_t)rb, ctx->stream));
     if (axes[k].prj_data) {
       s = upload_projections(r.get(), k, axes[k].prj_data, mem_kind);
       if (s != MTR_OK) return s;
@@ -751,10 +769,12 @@ mtr_status mtr_recon_describe(const mtr_recon* r, char* buf, int cap) {
     const AxisState& a = r->ax[k];
     char t[512];
     std::snprintf(t, sizeof(t),
-                  "%s{\"axis\":%zu,\"back_projection\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\"},"
+                  "%s{\"axis\":%zu,\"back_projection\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\","
+                  "\"window_format\":\"%s\"},"
                   "\"forward\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\",\"y_has_z\":%s}}",
                   k ? "," : "", k, a.tma ? "true" : "false", a.plan.nz, a.plan.WX, a.plan.WY,
-                  a.plan.lanes == 1 ? "y" : a.plan.lanes == 2 ? "patch" : "x", a.ftma ? "true" : "false", a.fplan.nz, a.fplan.WX, a.fplan.WY,
+                  a.plan.lanes == 1 ? "y" : a.plan.lanes == 2 ? "patch" : "x", a.plan.pairs ? "pairs" : "fp32",
+                  a.ftma ? "true" : "false", a.fplan.nz, a.fplan.WX, a.fplan.WY,
                   a.fplan.lanes == 1 ? "y" : a.fplan.lanes == 2 ? "patch" : "x", a.fplan.bz0 ? "false" : "true");
     s += t;
   }

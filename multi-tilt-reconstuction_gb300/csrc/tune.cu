@@ -9,16 +9,23 @@
 //  * warp layout: lines along X keep volume accesses coalesced, lines along
 //    the volume axis that detector x follows keep shared-memory gathers free
 //    of bank conflicts, and (back-projection) 8x4 patches keep the taps of an
-//    oblique axis compact in the window.
-// For each tilt axis the tuner times every candidate (depth 4/8/16 x lines
-// along X / lines along Y / patches for the SIRT back-projection, depth
-// 8/16/32 x the same three layouts for the forward splat) with CUDA events on the reconstruction's own buffers, before they
-// hold data (each candidate launch writes only scratch that the run
-// overwrites), and keeps the fastest.  Results are cached per process by a
-// geometry key and, when MTR_AUTOTUNE_CACHE names a file, persisted there as
-// JSON ({"key": [bp_depth, fwd_depth, bp_lane, fwd_lane], ...}).
-// MTR_AUTOTUNE=0 disables tuning (depths 8 and 16, lane axis by slope);
-// MTR_FORCE_DEPTHS=bp,fwd[,bp_lane,fwd_lane] pins the choice.
+//    oblique axis compact in the window;
+//  * the SIRT back-projection's window format: FP32 residual values, or
+//    (value, next - value) pairs that halve the tap loads but double the
+//    window and load 8 bytes per lane (faster where a warp's lanes share
+//    detector rows, slower where their 8-byte loads conflict in the banks).
+// For each tilt axis the tuner times every candidate (2 formats x depth
+// 4/8/16/32 x lines along X / lines along Y / patches for the SIRT
+// back-projection, depth 8/16/32 x the same three layouts for the forward
+// splat) with CUDA events on the reconstruction's own buffers, over at most
+// 32 Z planes, before they hold data (each candidate launch writes only
+// scratch that the run overwrites), and keeps the fastest.  Results are
+// cached per process by a geometry key and, when MTR_AUTOTUNE_CACHE names a
+// file, persisted there as JSON ({"key": [bp_depth, fwd_depth, bp_lane,
+// fwd_lane, bp_pairs], ...}).  MTR_AUTOTUNE=0 disables tuning (depths 8 and
+// 16, lane axis by slope, FP32 windows);
+// MTR_FORCE_DEPTHS=bp,fwd[,bp_lane,fwd_lane[,bp_pairs]] pins the choice.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -38,6 +45,7 @@ namespace {
 
 struct Choice {
   int bp_nz = 8, fwd_nz = 16, bp_lane = -1, fwd_lane = -1;
+  int bp_pairs = 0;  // SIRT update over residual-pair windows (1) or FP32 windows (0)
 };
 
 std::mutex g_mu;
@@ -68,7 +76,8 @@ void load_file() {
     const size_t lb = s.find('[', j), rb = s.find(']', j);
     if (lb == std::string::npos || rb == std::string::npos) break;
     Choice c;
-    if (std::sscanf(s.c_str() + lb, "[%d , %d , %d , %d]", &c.bp_nz, &c.fwd_nz, &c.bp_lane, &c.fwd_lane) == 4)
+    if (std::sscanf(s.c_str() + lb, "[%d , %d , %d , %d , %d]", &c.bp_nz, &c.fwd_nz, &c.bp_lane, &c.fwd_lane,
+                    &c.bp_pairs) == 5)
       g_cache[key] = c;
     i = rb + 1;
   }
@@ -83,7 +92,7 @@ void save_file() {
   size_t n = 0;
   for (const auto& kv : g_cache)
     f << "  \"" << kv.first << "\": [" << kv.second.bp_nz << ", " << kv.second.fwd_nz << ", " << kv.second.bp_lane
-      << ", " << kv.second.fwd_lane << "]" << (++n < g_cache.size() ? ",\n" : "\n");
+      << ", " << kv.second.fwd_lane << ", " << kv.second.bp_pairs << "]" << (++n < g_cache.size() ? ",\n" : "\n");
   f << "}\n";
 }
 
@@ -97,7 +106,7 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
   }
   char buf[256];
   // the trailing tag names the timing method, so choices cached by an older one are not reused
-  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t6", a.PX, a.PY,
+  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t7", a.PX, a.PY,
                 a.A, v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
   return buf;
 }
@@ -158,9 +167,10 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
   bool known = false;
   if (const char* f = std::getenv("MTR_FORCE_DEPTHS")) {
     Choice c;
-    const int n = std::sscanf(f, "%d,%d,%d,%d", &c.bp_nz, &c.fwd_nz, &c.bp_lane, &c.fwd_lane);
+    const int n = std::sscanf(f, "%d,%d,%d,%d,%d", &c.bp_nz, &c.fwd_nz, &c.bp_lane, &c.fwd_lane, &c.bp_pairs);
     if (n >= 2) {
       if (n < 4) c.bp_lane = c.fwd_lane = -1;
+      if (n < 5) c.bp_pairs = 0;
       ch = c;
       known = true;
     }
@@ -174,39 +184,55 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
       known = true;
     }
   }
-  const int z0 = v.Zs, z1 = v.Zs + v.NZ;
+  // Candidates are timed over a Z-slab of the frame with enough bricks for
+  // 8 waves of the deepest tile (32 planes, 3 CTAs per SM), at least 32
+  // planes: a launch's cost grows with its planes, but the ranking of tiles
+  // stays the frame's only while no tile runs a partly filled last wave.
+  VolDev tv = v;
+  {
+    const long long cols = (long long)((v.NX + 31) / 32) * ((v.NY + 7) / 8);  // bricks per 32-plane layer
+    const long long layers = (8LL * ctx->num_sms * 3 + cols - 1) / cols;
+    tv.NZ = (int)std::min<long long>(v.NZ, 32 * std::max(1LL, layers));
+  }
+  const int z0 = tv.Zs, z1 = tv.Zs + tv.NZ;
   if (!known && autotune_enabled()) {
     // Non-zero weight sums, so that every candidate's SIRT epilogue reads and
     // writes the volume as a real run does (with zeros it would skip the
     // update, hiding the cost of strided lanes-along-Y stores).
-    launch_fill(scratch_cbp, (long long)v.NX * v.NY * v.NZ, 1.f, ctx->stream);
-    // back-projection candidates: depth x lane axis
+    launch_fill(scratch_cbp, (long long)tv.NX * tv.NY * tv.NZ, 1.f, ctx->stream);
+    // back-projection candidates: window format x depth x lane axis
     std::vector<std::function<cudaError_t()>> cands;
-    std::vector<std::pair<int, int>> what;
+    std::vector<Choice> what;
     std::vector<BpPlan> bps;
     std::vector<CUtensorMap> bmaps;
     // (the candidates keep pointers into these: no reallocation)
-    bps.reserve(3 * std::size(kBpDepths));
-    bmaps.reserve(3 * std::size(kBpDepths));
-    for (int lane = 0; lane < 3; ++lane)
-      for (int nz : kBpDepths) {
-        BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, false, nz, lane);
-        CUtensorMap m;
-        if (!p.ok || !encode_tensor_map_3d(&m, a.r.p, false, a.PX, a.pitch, a.PY, a.A, p.WX, p.WY)) continue;
-        bps.push_back(p);
-        bmaps.push_back(m);
-        const BpPlan* pp = &bps.back();
-        const CUtensorMap* mp = &bmaps.back();
-        cands.push_back([=, &a, &v] {
-          return launch_backproject_tma<float>(*mp, *pp, a.dev(), v, 1, 0.5f, scratch_vol, scratch_cbp, scratch_copy,
-                                               copy_kind, z0, z1, err, ctx->stream);
-        });
-        what.push_back({nz, lane});
-      }
+    bps.reserve(6 * std::size(kBpDepths));
+    bmaps.reserve(6 * std::size(kBpDepths));
+    for (int pairs = 0; pairs < 2; ++pairs)
+      for (int lane = 0; lane < 3; ++lane)
+        for (int nz : kBpDepths) {
+          BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, pairs != 0, nz, lane);
+          CUtensorMap m;
+          if (!p.ok || !encode_residual_map(&m, a, p)) continue;
+          bps.push_back(p);
+          bmaps.push_back(m);
+          const BpPlan* pp = &bps.back();
+          const CUtensorMap* mp = &bmaps.back();
+          cands.push_back([=, &a, &tv] {
+            return launch_backproject_tma<float>(*mp, *pp, a.dev(), tv, 1, 0.5f, scratch_vol, scratch_cbp,
+                                                 scratch_copy, copy_kind, z0, z1, err, ctx->stream);
+          });
+          Choice c;
+          c.bp_nz = nz;
+          c.bp_lane = lane;
+          c.bp_pairs = pairs;
+          what.push_back(c);
+        }
     int k = fastest(ctx->stream, cands);
     if (k >= 0) {
-      ch.bp_nz = what[k].first;
-      ch.bp_lane = what[k].second;
+      ch.bp_nz = what[k].bp_nz;
+      ch.bp_lane = what[k].bp_lane;
+      ch.bp_pairs = what[k].bp_pairs;
     }
     // forward candidates
     cands.clear();
@@ -225,22 +251,25 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
         fmaps.push_back(m);
         const FwdPlan* pp = &fps.back();
         const CUtensorMap* mp = &fmaps.back();
-        cands.push_back([=, &a, &v] {
+        cands.push_back([=, &a, &tv] {
           if (copy_kind == 1)
-            return launch_forward_tma<__nv_bfloat16>(*mp, *pp, a.dev(), v,
+            return launch_forward_tma<__nv_bfloat16>(*mp, *pp, a.dev(), tv,
                                                      static_cast<const __nv_bfloat16*>(scratch_copy), z0, z1, err,
                                                      ctx->stream);
           if (copy_kind == 2)
-            return launch_forward_tma<__half>(*mp, *pp, a.dev(), v, static_cast<const __half*>(scratch_copy), z0, z1,
+            return launch_forward_tma<__half>(*mp, *pp, a.dev(), tv, static_cast<const __half*>(scratch_copy), z0, z1,
                                               err, ctx->stream);
-          return launch_forward_tma<float>(*mp, *pp, a.dev(), v, scratch_vol, z0, z1, err, ctx->stream);
+          return launch_forward_tma<float>(*mp, *pp, a.dev(), tv, scratch_vol, z0, z1, err, ctx->stream);
         });
-        what.push_back({nz, lane});
+        Choice c;
+        c.fwd_nz = nz;
+        c.fwd_lane = lane;
+        what.push_back(c);
       }
     k = fastest(ctx->stream, cands);
     if (k >= 0) {
-      ch.fwd_nz = what[k].first;
-      ch.fwd_lane = what[k].second;
+      ch.fwd_nz = what[k].fwd_nz;
+      ch.fwd_lane = what[k].fwd_lane;
     }
     std::lock_guard<std::mutex> lock(g_mu);
     g_cache[key] = ch;
@@ -248,9 +277,8 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
   }
   // the timing runs wrote into s and the tuner's scratch: restore the zeros
   cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream);
-  a.plan = plan_backproject(a.hxc, a.hyc, a.A, false, ch.bp_nz, ch.bp_lane);
-  a.tma = a.plan.ok &&
-          encode_tensor_map_3d(&a.map_r, a.r.p, false, a.PX, a.pitch, a.PY, a.A, a.plan.WX, a.plan.WY);
+  a.plan = plan_backproject(a.hxc, a.hyc, a.A, ch.bp_pairs != 0, ch.bp_nz, ch.bp_lane);
+  a.tma = a.plan.ok && encode_residual_map(&a.map_r, a, a.plan);
   a.fplan = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, ch.fwd_nz, ch.fwd_lane);
   a.ftma = a.fplan.ok &&
            encode_tensor_map_3d(&a.map_s, a.s.p, false, a.pitch, a.pitch, a.PY, a.A, a.fplan.WX, a.fplan.WY) &&
