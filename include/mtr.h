@@ -42,10 +42,12 @@ typedef enum mtr_status {
 } mtr_status;
 
 /* Storage precision.  FP32: everything float.  MIXED_*: projections stored
- * FP16, the volume copy read by the forward projector stored BF16 (or FP16);
- * interpolation and accumulation in FP32; residual norms and the MACE
- * consensus sum in FP64; the SIRT iterate, the residual and the MACE state
- * stay FP32. */
+ * FP16, the volume copy read by the forward projector stored BF16 (or FP16),
+ * the per-axis MACE states w_k stored FP16 (rounded once per outer
+ * iteration); interpolation and accumulation in FP32; residual norms and the
+ * MACE consensus sum in FP64; the SIRT iterate (updated every iteration), the
+ * residual, the weight sums and the consensus stay FP32.  Mixed storage takes
+ * less device memory than FP32; values must lie within the FP16 range. */
 typedef enum mtr_precision {
   MTR_PREC_FP32 = 0,
   MTR_PREC_MIXED_BF16 = 1,

@@ -34,6 +34,13 @@ __global__ void initial_z_kernel(const float* __restrict__ w, const float* __res
     z[i] = __fsub_rn(2.f * wavg[i], w[i]);
 }
 
+// The same from an FP16 state (mixed precision).
+__global__ void initial_z_half_kernel(const __half* __restrict__ w, const float* __restrict__ wavg,
+                                      float* __restrict__ z, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[i] = __fsub_rn(2.f * wavg[i], __half2float(w[i]));
+}
+
 // w = step*(2v - z) + (1-step)*w, with the reference host loop's float
 // rounding (MultiAxis.cpp:33-38; no fused multiply-add).
 __device__ __forceinline__ float mann(float v, float z, float w, float step) {
@@ -70,15 +77,37 @@ __global__ void widen_kernel(const __half* __restrict__ src, float* __restrict__
 //   wavg = (sum_k w[k]) / K      (summed in FP64)
 //   x[k] = 2 wavg - w[k]         (the next outer iteration's z_k)
 // and, when copy_kind != 0, x_copy[k] = x[k] in bf16/f16 for the forward pass.
-// dchange (optional, 2 doubles) accumulates sum (wavg_new - wavg_old)^2 and
-// sum wavg_new^2 in FP64: the convergence test's relative change.
+// With WH (mixed precision) the states w[k] are stored as FP16: each new w_k
+// is rounded to FP16 once, and that stored value is what the consensus and
+// the next z_k use.  REC: dchange (2 doubles) accumulates
+// sum (wavg_new - wavg_old)^2 and sum wavg_new^2 in FP64, the convergence
+// test's relative change (without it those FP64 operations are not run).
 constexpr int kMaxK = MTR_MAX_AXES;
 struct MacePtrs {
-  float* w[kMaxK];
+  void* w[kMaxK];
   float* x[kMaxK];
   void* xc[kMaxK];
 };
 
+template <bool WH>
+__device__ __forceinline__ float ld_state(const void* w, long long i) {
+  if constexpr (WH) return __half2float(static_cast<const __half*>(w)[i]);
+  else return static_cast<const float*>(w)[i];
+}
+// Stores the new state and returns the value stored.
+template <bool WH>
+__device__ __forceinline__ float st_state(void* w, long long i, float v) {
+  if constexpr (WH) {
+    const __half h = __float2half_rn(v);
+    static_cast<__half*>(w)[i] = h;
+    return __half2float(h);
+  } else {
+    static_cast<float*>(w)[i] = v;
+    return v;
+  }
+}
+
+template <bool REC, bool WH>
 __global__ void __launch_bounds__(kThreads)
 mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho, int copy_kind,
             double* __restrict__ dchange) {
@@ -91,18 +120,19 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
 #pragma unroll
     for (int k = 0; k < kMaxK; ++k) {
       if (k < K) {
-        const float wk = P.w[k][i];
+        const float wk = ld_state<WH>(P.w[k], i);
         const float zk = __fsub_rn(2.f * wa, wk);
-        wn[k] = mann(P.x[k][i], zk, wk, rho);
-        P.w[k][i] = wn[k];
+        wn[k] = st_state<WH>(P.w[k], i, mann(P.x[k][i], zk, wk, rho));
         sum += (double)wn[k];
       }
     }
     const float na = (float)(sum * inv_k);  // FP64 mean; the reciprocal spares an FP64 division
     wavg[i] = na;
-    const double d = (double)na - (double)wa;
-    acc += d * d;
-    acc2 += (double)na * (double)na;
+    if (REC) {
+      const double d = (double)na - (double)wa;
+      acc += d * d;
+      acc2 += (double)na * (double)na;
+    }
 #pragma unroll
     for (int k = 0; k < kMaxK; ++k) {
       if (k < K) {
@@ -113,7 +143,7 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
       }
     }
   }
-  if (dchange) {
+  if (REC) {
     for (int o = 16; o > 0; o >>= 1) {
       acc += __shfl_xor_sync(0xffffffffu, acc, o);
       acc2 += __shfl_xor_sync(0xffffffffu, acc2, o);
@@ -155,9 +185,9 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __re
 #pragma unroll
       for (int k = 0; k < kMaxK; ++k) {
         if (k < K) {
-          const float wk = D.w[k][i];
-          wn[k] = mann(D.x[k][i], __fsub_rn(2.f * wa, wk), wk, D.rho);
-          D.w[k][i] = wn[k];
+          const float wk = D.w_half ? ld_state<true>(D.w[k], i) : ld_state<false>(D.w[k], i);
+          const float wu = mann(D.x[k][i], __fsub_rn(2.f * wa, wk), wk, D.rho);
+          wn[k] = D.w_half ? st_state<true>(D.w[k], i, wu) : st_state<false>(D.w[k], i, wu);
           sum += (double)wn[k];
         }
       }
@@ -213,6 +243,9 @@ void launch_axpy_acc(float* dst, const float* src, long long n, cudaStream_t st)
 void launch_initial_z(const float* w, const float* wavg, float* z, long long n, cudaStream_t st) {
   initial_z_kernel<<<grid_for(n), kThreads, 0, st>>>(w, wavg, z, n);
 }
+void launch_initial_z_half(const __half* w, const float* wavg, float* z, long long n, cudaStream_t st) {
+  initial_z_half_kernel<<<grid_for(n), kThreads, 0, st>>>(w, wavg, z, n);
+}
 void launch_update_w(const float* v, const float* z, float* w, long long n, float step, cudaStream_t st) {
   update_w_kernel<<<grid_for(n), kThreads, 0, st>>>(v, z, w, n, step);
 }
@@ -222,15 +255,22 @@ void launch_convert_copy(const float* src, void* dst, int copy_kind, long long n
 void launch_widen(const __half* src, float* dst, long long n, cudaStream_t st) {
   widen_kernel<<<grid_for(n), kThreads, 0, st>>>(src, dst, n);
 }
-void launch_mace(int K, float* const* w, float* const* x, float* wavg, long long n, float rho, void* const* x_copy,
-                 int copy_kind, double* dchange, cudaStream_t st) {
+void launch_mace(int K, void* const* w, int w_half, float* const* x, float* wavg, long long n, float rho,
+                 void* const* x_copy, int copy_kind, double* dchange, cudaStream_t st) {
   MacePtrs P{};
   for (int k = 0; k < K && k < kMaxK; ++k) {
     P.w[k] = w[k];
     P.x[k] = x[k];
     P.xc[k] = x_copy ? x_copy[k] : nullptr;
   }
-  mace_kernel<<<grid_for(n), kThreads, 0, st>>>(K, P, wavg, n, rho, copy_kind, dchange);
+  const unsigned g = grid_for(n);
+  if (dchange) {
+    if (w_half) mace_kernel<true, true><<<g, kThreads, 0, st>>>(K, P, wavg, n, rho, copy_kind, dchange);
+    else mace_kernel<true, false><<<g, kThreads, 0, st>>>(K, P, wavg, n, rho, copy_kind, dchange);
+  } else {
+    if (w_half) mace_kernel<false, true><<<g, kThreads, 0, st>>>(K, P, wavg, n, rho, copy_kind, nullptr);
+    else mace_kernel<false, false><<<g, kThreads, 0, st>>>(K, P, wavg, n, rho, copy_kind, nullptr);
+  }
 }
 
 }  // namespace mtr

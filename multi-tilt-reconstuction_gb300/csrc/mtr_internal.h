@@ -207,7 +207,8 @@ struct ResBatchDesc {
 };
 struct MaceBatchDesc {
   int K;
-  float* w[MTR_MAX_AXES];
+  void* w[MTR_MAX_AXES];  // MACE states: FP32, or FP16 when w_half
+  int w_half;
   float* x[MTR_MAX_AXES];
   void* xc[MTR_MAX_AXES];
   float* wavg;
@@ -251,10 +252,12 @@ void launch_mace_batch(const MaceBatchDesc* descs, const long long* first, int n
 int device_sm_count();
 void launch_fill(float* p, long long n, float v, cudaStream_t st);
 void launch_axpy_acc(float* dst, const float* src, long long n, cudaStream_t st);  // dst += src
-// Fused MACE step over K axes (see mace.cu).
-void launch_mace(int K, float* const* w, float* const* x, float* wavg, long long n, float rho,
+// Fused MACE step over K axes (see mace.cu).  w: the K states, FP32 or
+// (w_half) FP16; dchange null: no convergence record.
+void launch_mace(int K, void* const* w, int w_half, float* const* x, float* wavg, long long n, float rho,
                  void* const* x_copy, int copy_kind, double* dchange, cudaStream_t st);
 void launch_initial_z(const float* w, const float* wavg, float* z, long long n, cudaStream_t st);
+void launch_initial_z_half(const __half* w, const float* wavg, float* z, long long n, cudaStream_t st);
 void launch_update_w(const float* v, const float* z, float* w, long long n, float step, cudaStream_t st);
 void launch_convert_copy(const float* src, void* dst, int copy_kind, long long n, cudaStream_t st);
 // dst[i] = (float)src[i]: FP16 projections widened for the FP32 WBP kernel.

@@ -45,6 +45,11 @@ long long residual_bytes(int PX, int PY, int A) {
   return std::max((long long)projection_pitch(PX) * PY * A * 4, (long long)pair_pitch(PX) * PY * A * 8);
 }
 
+// Bytes per voxel of an axis' MACE state w_k: FP32, or FP16 in mixed
+// precision (it changes once per outer iteration; the SIRT iterate x_k, which
+// accumulates an update every iteration, stays FP32).
+long long state_bytes(int precision) { return mixed(precision) ? 2 : 4; }
+
 long long axis_bytes(long long np, long long r_bytes, long long nv, int precision) {
   const long long pe = mixed(precision) ? 2 : 4;
   long long b = 0;
@@ -52,9 +57,21 @@ long long axis_bytes(long long np, long long r_bytes, long long nv, int precisio
   b += np * 4;        // s
   b += np * 4;        // cf
   b += r_bytes;       // r (FP32 values in every mode: the back-projection reads them per tap)
-  b += nv * 4 * 3;    // cbp, w, x
+  b += nv * 4 * 2;    // cbp, x
+  b += nv * state_bytes(precision);   // w
   if (mixed(precision)) b += nv * 2;  // xcopy
   return b;
+}
+
+// w_k = v (FP32 on the device): copied, or rounded to FP16 in mixed precision.
+mtr_status set_state(mtr_recon* r, AxisState& a, const float* v, cudaStream_t st) {
+  if (!mixed(r->p.precision)) {
+    MTR_CK(r->ctx, cudaMemcpyAsync(a.w.p, v, (size_t)r->nv * 4, cudaMemcpyDefault, st));
+    return MTR_OK;
+  }
+  launch_convert_copy(v, a.w.p, 2, r->nv, st);
+  MTR_CK_LAUNCH(r->ctx, "state copy");
+  return MTR_OK;
 }
 
 mtr_status check_params(mtr_context* ctx, const mtr_params& p) {
@@ -248,13 +265,20 @@ mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
     launch_axpy_acc(wavg, a.x.as<float>(), nv, ctx->stream);
     MTR_CK_LAUNCH(ctx, "initial model sum");
   }
-  // w_k = w_avg; first z_k = 2 w_avg - w_k = w_avg.
+  // w_k = w_avg; first z_k = 2 w_avg - w_k (= w_avg, up to the FP16 rounding
+  // of a mixed-precision state).
   for (auto& a : r->ax) {
-    MTR_CK(ctx, cudaMemcpyAsync(a.w.p, wavg, vbytes, cudaMemcpyDefault, ctx->stream));
-    MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDefault, ctx->stream));
+    mtr_status s = set_state(r, a, wavg, ctx->stream);
+    if (s != MTR_OK) return s;
+    if (mixed(r->p.precision)) {
+      launch_initial_z_half(a.w.as<__half>(), wavg, a.x.as<float>(), nv, ctx->stream);
+      MTR_CK_LAUNCH(ctx, "initial z");
+    } else {
+      MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDefault, ctx->stream));
+    }
     if (ck) {
       ProfScope ps(ctx, MTR_KERNEL_OTHER);
-      launch_convert_copy(wavg, a.xcopy.p, ck, nv, ctx->stream);
+      launch_convert_copy(a.x.as<float>(), a.xcopy.p, ck, nv, ctx->stream);
       MTR_CK_LAUNCH(ctx, "volume copy");
     }
   }
@@ -367,21 +391,20 @@ constexpr char kCkptMagic[8] = {'M', 'T', 'R', 'C', 'K', 'P', 'T', '1'};
 mtr_status mtr::recon_enqueue_mace(mtr_recon* r, int it) {
   mtr_context* ctx = r->ctx;
   const int K = r->K;
-  float* ws[MTR_MAX_AXES];
+  void* ws[MTR_MAX_AXES];
   float* xs[MTR_MAX_AXES];
   void* xcs[MTR_MAX_AXES];
   for (int k = 0; k < K; ++k) {
-    ws[k] = r->ax[k].w.as<float>();
+    ws[k] = r->ax[k].w.p;
     xs[k] = r->ax[k].x.as<float>();
     xcs[k] = r->ax[k].xcopy.p;
   }
-  double* dch = r->dchange.as<double>();
   {
     ProfScope ps(ctx, MTR_KERNEL_MACE);
     // the FP64 convergence sums cost five of the step's FP64 operations per
     // voxel: only when a record is kept
-    launch_mace(K, ws, xs, r->wavg.as<float>(), r->nv, r->p.mace_step, xcs, copy_kind_of(r->p.precision),
-                r->record_changes && dch && it < r->p.iter_times ? dch + 2 * it : nullptr, ctx->stream);
+    launch_mace(K, ws, mixed(r->p.precision) ? 1 : 0, xs, r->wavg.as<float>(), r->nv, r->p.mace_step, xcs,
+                copy_kind_of(r->p.precision), recon_change_slot(r, it), ctx->stream);
   }
   MTR_CK_LAUNCH(ctx, "mace");
   return MTR_OK;
@@ -471,7 +494,7 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
     const long long rb = residual_bytes(a.PX, a.PY, a.A);
     MTR_CK(ctx, a.r.alloc_pooled((size_t)rb, ctx));
     MTR_CK(ctx, a.cbp.alloc_where(vb, hv, ctx));
-    MTR_CK(ctx, a.w.alloc_where(vb, hv, ctx));
+    MTR_CK(ctx, a.w.alloc_where((size_t)(r->nv * state_bytes(params->precision)), hv, ctx));
     MTR_CK(ctx, a.x.alloc_where(vb, hv, ctx));
     if (mx) MTR_CK(ctx, a.xcopy.alloc_where((size_t)r->nv * 2, hv, ctx));
     r->bytes += axis_bytes(a.np, rb, hv ? 0 : r->nv, params->precision) + 64LL * a.A;  // device bytes
@@ -496,7 +519,8 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
         tune_axis(ctx, a, tv, params->precision, r->slabs->x[0].as<float>(), r->slabs->cbp[0].as<float>(),
                   r->slabs->xc[0].p, r->err.as<int>());
       } else {
-        tune_axis(ctx, a, r->vol, params->precision, a.w.as<float>(), a.cbp.as<float>(), a.xcopy.p,
+        // (x and cbp: FP32 volume arrays the WBP init writes afterwards)
+        tune_axis(ctx, a, r->vol, params->precision, a.x.as<float>(), a.cbp.as<float>(), a.xcopy.p,
                   r->err.as<int>());
       }
       // The WBP gathers the same windows as the SIRT update: the lane layout
@@ -568,11 +592,17 @@ mtr_status mtr_recon_save(mtr_recon* r, const char* path) {
   h.Z = r->vs.Z;
   h.outer_done = r->outer_done;
   h.precision = r->p.precision;
+  DevBuf tmp;  // FP32 view of an FP16 state (mixed precision)
+  if (mixed(r->p.precision)) MTR_CK(ctx, tmp.alloc_pooled(vb, ctx));
   FILE* f = std::fopen(path, "wb");
   if (!f) return set_error(ctx, MTR_ERR_IO, std::string("cannot create ") + path);
   bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
   for (int k = -1; ok && k < r->K; ++k) {
     const void* src = k < 0 ? r->wavg.p : r->ax[k].w.p;
+    if (k >= 0 && tmp.p) {  // the file holds FP32 states in every precision
+      launch_widen(r->ax[k].w.as<__half>(), tmp.as<float>(), r->nv, ctx->stream);
+      src = tmp.p;
+    }
     cudaError_t e = cudaMemcpyAsync(host.data(), src, vb, cudaMemcpyDefault, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
@@ -610,13 +640,28 @@ mtr_status mtr_recon_load(mtr_recon* r, const char* path, int* outer_done) {
   }
   const size_t vb = (size_t)r->nv * 4;
   std::vector<float> host((size_t)r->nv);
+  DevBuf tmp;  // FP32 staging of a state that is stored FP16 (mixed precision)
+  if (mixed(r->p.precision)) {
+    const cudaError_t e = tmp.alloc_pooled(vb, ctx);
+    if (e != cudaSuccess) {
+      std::fclose(f);
+      return cuda_error(ctx, e, "checkpoint staging");
+    }
+  }
   for (int k = -1; k < r->K; ++k) {
     if (std::fread(host.data(), 4, (size_t)r->nv, f) != (size_t)r->nv) {
       std::fclose(f);
       return set_error(ctx, MTR_ERR_FORMAT, "truncated checkpoint");
     }
-    void* dst = k < 0 ? r->wavg.p : r->ax[k].w.p;
+    void* dst = k < 0 ? r->wavg.p : (tmp.p ? tmp.p : r->ax[k].w.p);
     cudaError_t e = cudaMemcpyAsync(dst, host.data(), vb, cudaMemcpyDefault, ctx->stream);
+    if (e == cudaSuccess && k >= 0 && tmp.p) {
+      const mtr_status ss = set_state(r, r->ax[k], tmp.as<float>(), ctx->stream);
+      if (ss != MTR_OK) {
+        std::fclose(f);
+        return ss;
+      }
+    }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);  // host buffer is reused
     if (e != cudaSuccess) {
       std::fclose(f);
@@ -627,7 +672,10 @@ mtr_status mtr_recon_load(mtr_recon* r, const char* path, int* outer_done) {
   // next SIRT start z_k = 2 w_avg - w_k (as the MACE step leaves it) and its copy
   const int ck = copy_kind_of(r->p.precision);
   for (auto& a : r->ax) {
-    launch_initial_z(a.w.as<float>(), r->wavg.as<float>(), a.x.as<float>(), r->nv, ctx->stream);
+    if (mixed(r->p.precision))
+      launch_initial_z_half(a.w.as<__half>(), r->wavg.as<float>(), a.x.as<float>(), r->nv, ctx->stream);
+    else
+      launch_initial_z(a.w.as<float>(), r->wavg.as<float>(), a.x.as<float>(), r->nv, ctx->stream);
     MTR_CK_LAUNCH(ctx, "resume z");
     if (ck) {
       launch_convert_copy(a.x.as<float>(), a.xcopy.p, ck, r->nv, ctx->stream);
@@ -706,8 +754,24 @@ mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind) {
   DeviceGuard g(ctx->device);
   // (volume arrays may be mapped host memory: let unified addressing pick the direction)
   const cudaMemcpyKind kind = cudaMemcpyDefault;
-  for (int k = 0; k < r->K; ++k)
-    MTR_CK(ctx, cudaMemcpyAsync(out + (size_t)k * r->nv, r->ax[k].w.p, (size_t)r->nv * 4, kind, ctx->stream));
+  if (!mixed(r->p.precision)) {
+    for (int k = 0; k < r->K; ++k)
+      MTR_CK(ctx, cudaMemcpyAsync(out + (size_t)k * r->nv, r->ax[k].w.p, (size_t)r->nv * 4, kind, ctx->stream));
+  } else if (mem_kind == MTR_MEM_DEVICE) {  // FP16 states widened straight into the caller's array
+    for (int k = 0; k < r->K; ++k) {
+      launch_widen(r->ax[k].w.as<__half>(), out + (size_t)k * r->nv, r->nv, ctx->stream);
+      MTR_CK_LAUNCH(ctx, "widen state");
+    }
+  } else {
+    DevBuf tmp;
+    MTR_CK(ctx, tmp.alloc_pooled((size_t)r->nv * 4, ctx));
+    for (int k = 0; k < r->K; ++k) {
+      launch_widen(r->ax[k].w.as<__half>(), tmp.as<float>(), r->nv, ctx->stream);
+      MTR_CK_LAUNCH(ctx, "widen state");
+      MTR_CK(ctx, cudaMemcpyAsync(out + (size_t)k * r->nv, tmp.p, (size_t)r->nv * 4, kind, ctx->stream));
+    }
+    MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
+  }
   if (mem_kind != MTR_MEM_DEVICE) MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));
   return MTR_OK;
 }

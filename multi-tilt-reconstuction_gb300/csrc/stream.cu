@@ -129,33 +129,36 @@ mtr_status mace_pass(mtr_recon* r, int it) {
   const int K = r->K, ck = recon_copy_kind(r);
   mtr_status st = after(ctx, S, 2, c, S.out);  // the last update pass' copies out
   if (st != MTR_OK) return st;
+  // chunk layout: x_k (FP32) x K, w_avg (FP32), w_k (FP16 in mixed precision,
+  // else FP32) x K, forward copies (mixed) x K
   const long long cap = (long long)S.mace_planes * S.plane;
-  float* base = S.mace.as<float>();
-  float* ws[MTR_MAX_AXES];
+  const size_t ws_es = ck ? 2 : 4;
+  char* base = static_cast<char*>(S.mace.p);
+  void* ws[MTR_MAX_AXES];
   float* xs[MTR_MAX_AXES];
   void* xcs[MTR_MAX_AXES];
+  float* wa = reinterpret_cast<float*>(base + (long long)K * cap * 4);
+  char* wbase = base + (long long)(K + 1) * cap * 4;
   for (int k = 0; k < K; ++k) {
-    ws[k] = base + (long long)k * cap;
-    xs[k] = base + (long long)(K + k) * cap;
-    xcs[k] = ck ? static_cast<void*>(reinterpret_cast<char*>(base + (long long)(2 * K + 1) * cap) + (long long)k * cap * 2)
-                : nullptr;
+    xs[k] = reinterpret_cast<float*>(base + (long long)k * cap * 4);
+    ws[k] = wbase + (long long)k * cap * ws_es;
+    xcs[k] = ck ? static_cast<void*>(wbase + (long long)K * cap * ws_es + (long long)k * cap * 2) : nullptr;
   }
-  float* wa = base + (long long)2 * K * cap;
   for (int j = 0; j * S.mace_planes < r->vol.NZ; ++j) {
     const SlabRange R = slab_range(r, j, S.mace_planes);
-    const size_t nb = (size_t)R.n * 4;
+    const size_t nb = (size_t)R.n * 4, nw = (size_t)R.n * ws_es;
     for (int k = 0; k < K; ++k) {
-      MTR_CK(ctx, cudaMemcpyAsync(ws[k], bytes_at(r->ax[k].w, R.off, 4), nb, cudaMemcpyDefault, c));
+      MTR_CK(ctx, cudaMemcpyAsync(ws[k], bytes_at(r->ax[k].w, R.off, ws_es), nw, cudaMemcpyDefault, c));
       MTR_CK(ctx, cudaMemcpyAsync(xs[k], bytes_at(r->ax[k].x, R.off, 4), nb, cudaMemcpyDefault, c));
     }
     MTR_CK(ctx, cudaMemcpyAsync(wa, bytes_at(r->wavg, R.off, 4), nb, cudaMemcpyDefault, c));
     {
       ProfScope ps(ctx, MTR_KERNEL_MACE);
-      launch_mace(K, ws, xs, wa, R.n, r->p.mace_step, xcs, ck, recon_change_slot(r, it), c);
+      launch_mace(K, ws, ck ? 1 : 0, xs, wa, R.n, r->p.mace_step, xcs, ck, recon_change_slot(r, it), c);
     }
     MTR_CK_LAUNCH(ctx, "mace (streamed)");
     for (int k = 0; k < K; ++k) {
-      MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].w, R.off, 4), ws[k], nb, cudaMemcpyDefault, c));
+      MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].w, R.off, ws_es), ws[k], nw, cudaMemcpyDefault, c));
       MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].x, R.off, 4), xs[k], nb, cudaMemcpyDefault, c));
       if (ck)
         MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].xcopy, R.off, 2), xcs[k], (size_t)R.n * 2, cudaMemcpyDefault,
@@ -189,9 +192,10 @@ mtr_status mtr::stream_setup(mtr_recon* r) {
   }
   MTR_CK(ctx, S->acc.alloc_pooled((size_t)sv * 4, ctx));
   bytes += sv * 4;
-  // A MACE chunk holds 2K + 1 FP32 planes sets (w_k, x_k, w_avg) and K
-  // forward copies per voxel: sized to about one slot's bytes.
-  const long long mace_voxel_bytes = (2LL * K + 1) * 4 + (ck ? 2LL * K : 0);
+  // A MACE chunk holds K + 1 FP32 volumes (x_k, w_avg), the K states w_k
+  // (FP16 in mixed precision) and K forward copies (mixed) per voxel: sized
+  // to about one slot's bytes.
+  const long long mace_voxel_bytes = (K + 1LL) * 4 + (ck ? 2LL * K + 2LL * K : 4LL * K);
   S->mace_planes = (int)std::max(1LL, std::min<long long>(NZ, S->depth * (ck ? 10LL : 8LL) / mace_voxel_bytes));
   const long long mv = (long long)S->mace_planes * S->plane;
   MTR_CK(ctx, S->mace.alloc_pooled((size_t)(mv * mace_voxel_bytes), ctx));
@@ -239,12 +243,22 @@ mtr_status mtr::stream_enqueue_init(mtr_recon* r) {
       }
     }
     MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->wavg, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
-    for (int k = 0; k < K; ++k) {
-      MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].w, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
-      MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].x, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
-    }
-    if (ck) {
-      launch_convert_copy(S.acc.as<float>(), S.xc[0].p, ck, R.n, c);
+    if (!ck) {  // w_k = x_k = w_avg
+      for (int k = 0; k < K; ++k) {
+        MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].w, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
+        MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].x, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
+      }
+    } else {  // w_k = w_avg in FP16, x_k = 2 w_avg - w_k, and the forward copies
+      launch_convert_copy(S.acc.as<float>(), S.xc[0].p, 2, R.n, c);
+      MTR_CK_LAUNCH(ctx, "state copy (streamed)");
+      launch_initial_z_half(S.xc[0].as<__half>(), S.acc.as<float>(), S.x[0].as<float>(), R.n, c);
+      MTR_CK_LAUNCH(ctx, "initial z (streamed)");
+      for (int k = 0; k < K; ++k) {
+        MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].w, R.off, 2), S.xc[0].p, (size_t)R.n * 2, cudaMemcpyDefault,
+                                    c));
+        MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].x, R.off, 4), S.x[0].p, nb, cudaMemcpyDefault, c));
+      }
+      launch_convert_copy(S.x[0].as<float>(), S.xc[0].p, ck, R.n, c);
       MTR_CK_LAUNCH(ctx, "volume copy (streamed)");
       for (int k = 0; k < K; ++k)
         MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].xcopy, R.off, 2), S.xc[0].p, (size_t)R.n * 2,
