@@ -469,6 +469,14 @@ typedef struct mtr_xf {
 } mtr_xf;
 mtr_status mtr_geometry_from_tilts(int n_views, const double* tilt_deg, const mtr_xf* xf, double phi_deg, int det_x,
                                    int det_y, mtr_volume_size vol, double* x_coef, double* y_coef);
+/* Writes n_views linear maps (4 doubles per view each, TXBR coefficient
+ * order) and the volume bounds of vol as a TXBR file in the grammar that
+ * mtr_txbr_read and the reference's readCoef (MrcFileIOBaseFunction.cpp:72-134)
+ * parse, every coefficient reading back exactly: maps built by
+ * mtr_geometry_from_tilts from IMOD .tlt / .xf files become inputs of the
+ * reference's command line (-i K,stacks,maps). */
+mtr_status mtr_txbr_write(const char* path, int n_views, const double* x_coef, const double* y_coef,
+                          mtr_volume_size vol);
 /* One angle per line (IMOD .tlt); reads up to cap values into *n. */
 mtr_status mtr_tlt_read(const char* path, double* tilt_deg, int cap, int* n);
 /* Six numbers per line "a11 a12 a21 a22 dx dy" (IMOD .xf); up to cap views. */

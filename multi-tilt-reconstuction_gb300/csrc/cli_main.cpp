@@ -6,8 +6,10 @@
 //
 //   mtr_multiaxis -i K,a.st,...,a.txbr,... -o out.mrc [-n 5] [-s 0.5] [-m 0.7]
 //                 [--inner 10] [--precision fp32|bf16|fp16]
+//   mtr_multiaxis tilts2txbr TLT OUT DET_X DET_Y XS XE YS YE ZS ZE [PHI_DEG [XF]]
 #include <chrono>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -36,9 +38,49 @@ int fail(const char* what, mtr_status s, const char* detail = nullptr) {
   return 1;
 }
 
+// mtr_multiaxis tilts2txbr TLT OUT DET_X DET_Y XS XE YS YE ZS ZE [PHI_DEG [XF]]
+// The linear maps of a parallel-beam tilt series (IMOD .tlt angles, optional
+// .xf alignments, tilt axis at in-plane angle PHI) over the volume frame
+// [XS,XE) x [YS,YE) x [ZS,ZE), written as a TXBR file for -i.
+int tilts_to_txbr(int argc, char** argv) {
+  if (argc < 12 || argc > 14) {
+    std::fprintf(stderr, "usage: mtr_multiaxis tilts2txbr TLT OUT DET_X DET_Y XS XE YS YE ZS ZE [PHI_DEG [XF]]\n");
+    return 2;
+  }
+  const int cap = 100000;
+  std::vector<double> tilt((size_t)cap);
+  int n = 0;
+  mtr_status s = mtr_tlt_read(argv[2], tilt.data(), cap, &n);
+  if (s != MTR_OK) return fail("read .tlt", s, argv[2]);
+  std::vector<mtr_xf> xf;
+  if (argc == 14) {
+    xf.resize((size_t)cap);
+    int nx = 0;
+    s = mtr_xf_read(argv[13], xf.data(), cap, &nx);
+    if (s != MTR_OK) return fail("read .xf", s, argv[13]);
+    if (nx != n) return fail(".xf", MTR_ERR_FORMAT, "one transform per tilt angle is needed");
+  }
+  int v[8];
+  for (int i = 0; i < 8; ++i) {
+    char* end = nullptr;
+    v[i] = (int)std::strtol(argv[4 + i], &end, 10);
+    if (!end || *end) return fail("arguments", MTR_ERR_INVALID_ARGUMENT, argv[4 + i]);
+  }
+  const double phi = argc >= 13 ? std::strtod(argv[12], nullptr) : 0.0;
+  mtr_volume_size vol{v[2], v[3], v[4], v[5], v[6], v[7], v[3] - v[2], v[5] - v[4], v[7] - v[6]};
+  std::vector<double> xc(4 * (size_t)n), yc(4 * (size_t)n);
+  s = mtr_geometry_from_tilts(n, tilt.data(), xf.empty() ? nullptr : xf.data(), phi, v[0], v[1], vol, xc.data(),
+                              yc.data());
+  if (s != MTR_OK) return fail("geometry", s);
+  s = mtr_txbr_write(argv[3], n, xc.data(), yc.data(), vol);
+  if (s != MTR_OK) return fail("write TXBR", s, argv[3]);
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
+  if (argc > 1 && std::strcmp(argv[1], "tilts2txbr") == 0) return tilts_to_txbr(argc, argv);
   mtr_options opt;
   mtr_status s = mtr_parse_options(argc, argv, &opt);
   if (s != MTR_OK) {

@@ -16,6 +16,7 @@
 //    header fields it leaves uninitialised are zero.
 #include <algorithm>
 #include <cerrno>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -257,6 +258,48 @@ mtr_status mtr_txbr_read(const char* path, double* x_coef, double* y_coef, int c
   *n_y = ny;
   if (nx > cap || ny > cap) return MTR_ERR_CAPACITY;
   return MTR_OK;
+}
+
+// The grammar mtr_txbr_read (and the reference's readCoef,
+// MrcFileIOBaseFunction.cpp:72-134) parses: per view an "l k" line and
+// "x-k:" / "y-k:" lines of the four coefficients [const, X, Y, Z], then the
+// "x->start:1:end" bound lines (fields 2 and 4 are start and end).  Numbers
+// are the shortest text that reads back to the same double (std::to_chars:
+// independent of the C locale), and no line ends in a blank (the reference
+// would read a trailing blank as one more coefficient).
+mtr_status mtr_txbr_write(const char* path, int n_views, const double* x_coef, const double* y_coef,
+                          mtr_volume_size vol) {
+  if (!path || n_views <= 0 || !x_coef || !y_coef) return MTR_ERR_INVALID_ARGUMENT;
+  for (int i = 0; i < 4 * n_views; ++i)
+    if (!std::isfinite(x_coef[i]) || !std::isfinite(y_coef[i])) return MTR_ERR_INVALID_ARGUMENT;
+  if (vol.Xend <= vol.Xstart || vol.Yend <= vol.Ystart || vol.Zend <= vol.Zstart) return MTR_ERR_INVALID_ARGUMENT;
+  std::string out;
+  out.reserve((size_t)n_views * 220 + 64);
+  char num[64];
+  auto append_num = [&](double v) {
+    const std::to_chars_result r = std::to_chars(num, num + sizeof num, v);
+    out.append(num, r.ptr);
+  };
+  for (int k = 0; k < n_views; ++k) {
+    const std::string label = std::to_string(k);
+    out += "l " + label + "\n";
+    for (int m = 0; m < 2; ++m) {
+      const double* c = (m == 0 ? x_coef : y_coef) + 4 * k;
+      out += (m == 0 ? "x-" : "y-") + label + ":";
+      for (int j = 0; j < 4; ++j) {
+        out += ' ';
+        append_num(c[j]);
+      }
+      out += '\n';
+    }
+  }
+  out += "x->" + std::to_string(vol.Xstart) + ":1:" + std::to_string(vol.Xend) + "\n";
+  out += "y->" + std::to_string(vol.Ystart) + ":1:" + std::to_string(vol.Yend) + "\n";
+  out += "z->" + std::to_string(vol.Zstart) + ":1:" + std::to_string(vol.Zend) + "\n";
+  File f(path, "wb");
+  if (!f.f) return MTR_ERR_IO;
+  if (std::fwrite(out.data(), 1, out.size(), f.f) != out.size()) return MTR_ERR_IO;
+  return std::fflush(f.f) == 0 ? MTR_OK : MTR_ERR_IO;
 }
 
 mtr_status mtr_mrc_write_volume(const char* path, mtr_volume_size vol, const float* data) {

@@ -163,6 +163,7 @@ _SIGNATURES = {
     "mtr_geometry_from_tilts": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(XF), C.c_double, C.c_int, C.c_int,
                                            VolumeSize, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "mtr_tlt_read": (C.c_int, [C.c_char_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int)]),
+    "mtr_txbr_write": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double), VolumeSize]),
     "mtr_xf_read": (C.c_int, [C.c_char_p, C.POINTER(XF), C.c_int, C.POINTER(C.c_int)]),
     "mtr_server_create": (C.c_int, [_P, C.c_longlong, C.c_int, C.POINTER(_P)]),
     "mtr_server_submit": (C.c_int, [_P, C.POINTER(RequestC), C.POINTER(C.c_longlong)]),
@@ -660,6 +661,17 @@ def geometry_from_tilts(tilt_deg, phi_deg: float, det_x: int, det_y: int, vol: V
     _check(load().mtr_geometry_from_tilts(n, t.ctypes.data_as(dp), xfa, float(phi_deg), det_x, det_y, vol,
                                           xs.ctypes.data_as(dp), ys.ctypes.data_as(dp)), "mtr_geometry_from_tilts")
     return xs, ys
+
+
+def write_txbr(path: str, x_coef, y_coef, vol: VolumeSize) -> None:
+    """TXBR file of the per-view maps (4 coefficients per view each) and vol's bounds."""
+    x = np.ascontiguousarray(x_coef, np.float64).reshape(-1)
+    y = np.ascontiguousarray(y_coef, np.float64).reshape(-1)
+    if x.size != y.size or x.size % 4:
+        raise ValueError("write_txbr: x and y maps need 4 coefficients per view each")
+    dp = C.POINTER(C.c_double)
+    _check(load().mtr_txbr_write(str(path).encode(), x.size // 4, x.ctypes.data_as(dp), y.ctypes.data_as(dp), vol),
+           "mtr_txbr_write")
 
 
 def read_tlt(path: str, cap: int = 100000) -> np.ndarray:

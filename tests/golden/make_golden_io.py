@@ -48,6 +48,13 @@ def run(*args) -> dict:
     return json.loads(line[5:])
 
 
+# Inputs of the libmtr-written TXBR record (also used by tests/test_io.py).
+TXBR_WRITTEN = dict(tilts=[-58.0, -41.5, -20.25, 0.0, 17.75, 39.0, 61.5], phi=37.5, det=(96, 80),
+                    vol=(-10, 70, 3, 61, -6, 18),
+                    xf=[[np.cos(0.02 * k), -np.sin(0.02 * k), np.sin(0.02 * k), np.cos(0.02 * k), 0.3 * k - 1.0,
+                         -0.45 * k + 0.7] for k in range(7)])
+
+
 class V:
     def __init__(self, xs, xe, ys, ye, zs, ze):
         self.Xstart, self.Xend, self.Ystart, self.Yend, self.Zstart, self.Zend = xs, xe, ys, ye, zs, ze
@@ -72,6 +79,18 @@ def main() -> None:
     # trailing blank before the newline: the reference appends a spurious 0 coefficient
     (OUT / "map_trailing_blank.txbr").write_text(phantom.txbr_text(xc, yc, vol).replace("\n", " \n", 2))
     rec["read_trailing_blank"] = run("read", OUT / "stack_mode1.st", OUT / "map_trailing_blank.txbr")
+    # a TXBR file written by libmtr (maps of a tilt series with 2-D alignments,
+    # mtr_geometry_from_tilts) as the reference's readCoef parses it
+    import mtr
+
+    tw = TXBR_WRITTEN
+    vw = mtr.VolumeSize.make(*tw["vol"])
+    xw, yw = mtr.geometry_from_tilts(tw["tilts"], tw["phi"], tw["det"][0], tw["det"][1], vw, xf=tw["xf"])
+    mtr.write_txbr(OUT / "written.txbr", xw, yw, vw)
+    stack_w = np.random.default_rng(2025).integers(-30000, 30000, size=(len(tw["tilts"]), 12, 12)).astype(np.int16)
+    (OUT / "stack_written.st").write_bytes(mrc_bytes(stack_w, 1))
+    rec["read_written"] = run("read", OUT / "stack_written.st", OUT / "written.txbr")
+    rec["read_written"].pop("data")
     # --- options --------------------------------------------------------------------
     rec["options"] = {
         "full": run("options", "MultiAxis", "-i", "2,a.st,b.st,a.txbr,b.txbr", "-o", "out.mrc", "-n", "3", "-s",

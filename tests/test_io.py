@@ -183,3 +183,58 @@ def test_txbr_writer_round_trip(tmp_path):
     np.testing.assert_array_equal(x, xc)
     np.testing.assert_array_equal(y, yc)
     assert v.astuple() == vol.astuple()
+
+
+def _written_inputs():
+    """Inputs of the libmtr-written TXBR record (make_golden_io.TXBR_WRITTEN)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden_io", Path(__file__).parent / "golden" / "make_golden_io.py")
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.TXBR_WRITTEN
+
+
+def test_txbr_written_by_libmtr_is_read_by_the_reference_exactly(rec, tmp_path):
+    """Maps of a tilt series with 2-D alignments (mtr_geometry_from_tilts),
+    written by mtr_txbr_write: the reference's readCoef read the committed file
+    (its record) back to exactly these coefficients and bounds, and libmtr
+    still writes that file byte for byte."""
+    tw = _written_inputs()
+    vol = mtr.VolumeSize.make(*tw["vol"])
+    xc, yc = mtr.geometry_from_tilts(tw["tilts"], tw["phi"], tw["det"][0], tw["det"][1], vol, xf=tw["xf"])
+    p = tmp_path / "w.txbr"
+    mtr.write_txbr(p, xc, yc, vol)
+    assert p.read_bytes() == (IO / "written.txbr").read_bytes()
+    r = rec["read_written"]
+    assert r["read_rc"] == 1 and r["prj"][2] == len(tw["tilts"])
+    np.testing.assert_array_equal(np.array(r["x_coef"]), xc)
+    np.testing.assert_array_equal(np.array(r["y_coef"]), yc)
+    assert tuple(r["vol"]) == vol.astuple()
+    x, y, v = mtr.read_txbr(str(p), len(xc))  # and libmtr's reader agrees
+    np.testing.assert_array_equal(x, xc)
+    assert v.astuple() == vol.astuple()
+
+
+def test_cli_converts_tilts_and_alignments_to_txbr(tmp_path):
+    tw = _written_inputs()
+    (tmp_path / "s.tlt").write_text("\n".join(repr(t) for t in tw["tilts"]) + "\n")
+    (tmp_path / "s.xf").write_text("\n".join(" ".join(repr(float(v)) for v in row) for row in tw["xf"]) + "\n")
+    cli = mtr.PKG / "bin" / "mtr_multiaxis"
+    import subprocess
+
+    args = [str(cli), "tilts2txbr", str(tmp_path / "s.tlt"), str(tmp_path / "o.txbr"), *map(str, tw["det"]),
+            *map(str, tw["vol"]), repr(tw["phi"]), str(tmp_path / "s.xf")]
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "o.txbr").read_bytes() == (IO / "written.txbr").read_bytes()
+    r = subprocess.run([str(cli), "tilts2txbr", str(tmp_path / "s.tlt")], capture_output=True, text=True)
+    assert r.returncode != 0
+
+
+def test_txbr_writer_rejects_bad_input(tmp_path):
+    vol = mtr.VolumeSize.make(0, 4, 0, 4, 0, 2)
+    with pytest.raises(mtr.MtrError):
+        mtr.write_txbr(tmp_path / "x.txbr", [np.nan, 1, 0, 0], [0, 0, 1, 0], vol)
+    with pytest.raises(mtr.MtrError):
+        mtr.write_txbr(tmp_path / "x.txbr", [0, 1, 0, 0], [0, 0, 1, 0], mtr.VolumeSize.make(0, 0, 0, 4, 0, 2))
