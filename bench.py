@@ -826,7 +826,8 @@ def main() -> int:
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": cfg["workload"], "precision": args.precision,
                        "storage": f"{args.precision} volume copy for the forward pass, fp16 projections, "
-                                  "fp32 iterate/residual/MACE state" if args.precision != "fp32"
+                                  "fp16 MACE states, fp32 iterate/residual/weight sums/consensus"
+                                  if args.precision != "fp32"
                        else "fp32", "voxel_updates_per_step": r["vu"], "parallelism": f"replicas x{world}",
                        "l2": l2_note(cfg),
                        "seed": cfg["seed"],
