@@ -78,8 +78,9 @@ __global__ void widen_kernel(const __half* __restrict__ src, float* __restrict__
 //   x[k] = 2 wavg - w[k]         (the next outer iteration's z_k)
 // and, when copy_kind != 0, x_copy[k] = x[k] in bf16/f16 for the forward pass.
 // With WH (mixed precision) the states w[k] are stored as FP16: each new w_k
-// is rounded to FP16 once, and that stored value is what the consensus and
-// the next z_k use.  REC: dchange (2 doubles) accumulates
+// is rounded to FP16 once when stored, and the next z_k uses the stored value
+// (the next step recomputes z_k from it); the consensus averages the unrounded
+// FP32 states, so the output carries no rounding of the step that made it.  REC: dchange (2 doubles) accumulates
 // sum (wavg_new - wavg_old)^2 and sum wavg_new^2 in FP64, the convergence
 // test's relative change (without it those FP64 operations are not run).
 constexpr int kMaxK = MTR_MAX_AXES;
@@ -122,8 +123,9 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
       if (k < K) {
         const float wk = ld_state<WH>(P.w[k], i);
         const float zk = __fsub_rn(2.f * wa, wk);
-        wn[k] = st_state<WH>(P.w[k], i, mann(P.x[k][i], zk, wk, rho));
-        sum += (double)wn[k];
+        const float wu = mann(P.x[k][i], zk, wk, rho);
+        wn[k] = st_state<WH>(P.w[k], i, wu);
+        sum += (double)wu;
       }
     }
     const float na = (float)(sum * inv_k);  // FP64 mean; the reciprocal spares an FP64 division
@@ -188,7 +190,7 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __re
           const float wk = D.w_half ? ld_state<true>(D.w[k], i) : ld_state<false>(D.w[k], i);
           const float wu = mann(D.x[k][i], __fsub_rn(2.f * wa, wk), wk, D.rho);
           wn[k] = D.w_half ? st_state<true>(D.w[k], i, wu) : st_state<false>(D.w[k], i, wu);
-          sum += (double)wn[k];
+          sum += (double)wu;
         }
       }
       const float na = (float)(sum * inv_k);  // FP64 mean; the reciprocal spares an FP64 division
