@@ -8,9 +8,10 @@ with inputs resident in HBM.  voxel-updates per step = V * K * n_outer * n_inner
     python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2] [--impl ours|reference]
 
 The default workload is the 3-axis 512x512x128 MACE configuration; the
-headline value is the mixed-precision path (BF16 volume copy, FP16
-projections/residuals, FP32 interpolation/accumulation, FP64 norms and
-consensus), with the plain FP32 path timed beside it.  Multi-GPU runs are
+headline value is the mixed-precision path (BF16 volume copy for the forward
+splat, FP16 projections and MACE states, FP32 interpolation, accumulation,
+iterate and residual, FP64 consensus sum), with the plain FP32 path timed
+beside it.  Multi-GPU runs are
 independent replicas (the reconstruction is not sharded across GPUs).
 """
 from __future__ import annotations
@@ -54,8 +55,8 @@ CONFIGS = {
 # Per-launch DRAM traffic and instruction count of the dominant kernel, from
 # the ncu captures summarised in profiles/ (one launch of axis 0).
 NCU_PROFILES = {
-    ("c2", "backproject"): {"traffic": 330_625_024 + 161_167_872, "warp_inst": 1_252_056_806,
-                            "duration_ms": 1.107520, "sm_ghz": 2.072, "sms": 152,
+    ("c2", "backproject"): {"traffic": 390_982_656 + 167_104_768, "warp_inst": 828_349_812,
+                            "duration_ms": 0.937248, "sm_ghz": 2.070, "sms": 152,
                             "source": "profiles/bp_tma_kernel_3axis_512x512x128.md"},
     ("c2", "forward"): {"traffic": 128_427_776 + 37_460_736, "warp_inst": 1_515_418_200,
                         "duration_ms": 1.537952, "sm_ghz": 2.061, "sms": 152,
@@ -299,9 +300,15 @@ def run_ours(args, rank: int, world: int, local_rank: int) -> dict | None:
     prec = {"bf16": mtr.PREC_MIXED_BF16, "fp16": mtr.PREC_MIXED_FP16, "fp32": mtr.PREC_FP32}[args.precision]
     mk = lambda pr: mtr.params(iter_times=no, sirt_inner=ni, sirt_step=cfg["sirt_step"], mace_step=cfg["mace_step"],
                                precision=pr)
-    rec = mtr.Recon(ctx, axes, vol, mk(prec), mem_kind=mtr.MEM_DEVICE)
+
+    def mk_timed(pr):  # the device-resident runs replay one CUDA graph per run
+        p = mk(pr)
+        p.flags = mtr.FLAG_GRAPH if args.graph else 0
+        return p
+
+    rec = mtr.Recon(ctx, axes, vol, mk_timed(prec), mem_kind=mtr.MEM_DEVICE)
     tiles = rec.describe()
-    ref32 = mtr.Recon(ctx, axes, vol, mk(mtr.PREC_FP32), mem_kind=mtr.MEM_DEVICE) if prec != mtr.PREC_FP32 else rec
+    ref32 = mtr.Recon(ctx, axes, vol, mk_timed(mtr.PREC_FP32), mem_kind=mtr.MEM_DEVICE) if prec != mtr.PREC_FP32 else rec
 
     def barrier():
         if world > 1:
@@ -758,6 +765,8 @@ def main() -> int:
     ap.add_argument("--fp64", type=int, default=1, help="1: state both paths' error against the FP64 GPU run")
     ap.add_argument("--extras", type=int, default=1,
                     help="1: also time the naive global-atomic kernels, host-resident volumes and MRC loading (c1/c2)")
+    ap.add_argument("--graph", type=int, default=1,
+                    help="1: the device-resident timed runs replay a CUDA graph of the whole run")
     ap.add_argument("--stream-slabs", type=int, default=0,
                     help="D > 0: also time the streaming slab loop (volume arrays in host memory, D-plane slabs)")
     args = ap.parse_args()

@@ -92,7 +92,9 @@ typedef struct mtr_params {
 
 /* Record the squared residual norm (FP64) of every SIRT iteration. */
 #define MTR_FLAG_RECORD_NORMS 1
-/* Capture the MACE outer iteration in a CUDA graph and replay it. */
+/* Capture a whole run (WBP init and every MACE iteration) in a CUDA graph on
+ * the first mtr_recon_run and replay it on the next ones.  Ignored while
+ * per-kernel profiling is on (mtr_context_set_profiling). */
 #define MTR_FLAG_GRAPH 2
 /* Keep the volume-sized arrays (iterates, MACE states, weight sums, forward
  * copies, consensus: 12-14 B per voxel and axis) in pinned host memory mapped

@@ -693,8 +693,9 @@ mtr_status mtr_recon_run(mtr_recon* r) {
   mtr_context* ctx = r->ctx;
   DeviceGuard g(ctx->device);
   r->outer_done = r->p.iter_times;
-  // (a streamed run waits on copies between its streams: not captured)
-  if (!(r->p.flags & MTR_FLAG_GRAPH) || r->slabs) return enqueue_run(r);
+  // (a streamed run waits on copies between its streams: not captured; with
+  // per-kernel profiling on, the launches run one by one between their events)
+  if (!(r->p.flags & MTR_FLAG_GRAPH) || r->slabs || ctx->profiling) return enqueue_run(r);
   if (!r->graph) {
     cudaGraph_t graph = nullptr;
     MTR_CK(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));

@@ -78,9 +78,20 @@ def test_graph_replay_matches_direct(ctx):
     first = r.download()
     r.run()  # replay
     second = r.download()
+    # per-kernel profiling runs the launches one by one, between their events
+    ctx.profile_reset()
+    ctx.set_profiling(True)
+    try:
+        r.run()
+        third = r.download()
+    finally:
+        ctx.set_profiling(False)
+    prof = ctx.profile()
     r.close()
     assert rel_l2(first, direct) < 1e-5
     assert rel_l2(second, first) < 1e-5
+    assert rel_l2(third, first) < 1e-5
+    assert prof["forward"][0] == 2 * 2 * 3 and prof["backproject"][0] > 0
 
 
 def test_residual_norms_decrease_and_match_oracle(ctx):
