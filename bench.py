@@ -8,11 +8,11 @@ with inputs resident in HBM.  voxel-updates per step = V * K * n_outer * n_inner
     python bench.py [--gpus N] [--steps K] [--warmup W] [--config c2] [--impl ours|reference]
 
 The default workload is the 3-axis 512x512x128 MACE configuration; the
-headline value is the mixed-precision path (BF16 volume copy for the forward
-splat, FP16 projections and MACE states, FP32 interpolation, accumulation,
-iterate and residual, FP64 consensus sum), with the plain FP32 path timed
-beside it.  Multi-GPU runs are
-independent replicas (the reconstruction is not sharded across GPUs).
+headline value is the mixed-precision path (FP16 volume copy for the forward
+splat, BF16 with --precision bf16; FP16 projections and MACE-state
+deviations; FP32 interpolation, accumulation, iterate and residual; FP64
+consensus sum), with the plain FP32 path timed beside it.  Multi-GPU runs
+are independent replicas (the reconstruction is not sharded across GPUs).
 """
 from __future__ import annotations
 
@@ -262,9 +262,9 @@ def algorithmic_bytes(kind: str, cfg: dict, prec: int) -> tuple[float, str]:
     P = cfg["px"] * cfg["px"] * n_angles(cfg)
     pe = 2 if prec != mtr.PREC_FP32 else 4
     if kind == "backproject":
-        # read r (FP32, P), read+write the FP32 iterate, read the weight sums (+ write the bf16 copy when mixed)
+        # read r (FP32, P), read+write the FP32 iterate, read the weight sums (+ write the 16-bit copy when mixed)
         b = P * 4 + V * 12 + (V * 2 if prec != mtr.PREC_FP32 else 0)
-        return b, f"P*4 (residual) + V*12 (iterate r/w, weight sums){' + V*2 (bf16 copy)' if pe == 2 else ''}"
+        return b, f"P*4 (residual) + V*12 (iterate r/w, weight sums){' + V*2 (16-bit copy)' if pe == 2 else ''}"
     if kind == "forward":
         vb = 2 if prec != mtr.PREC_FP32 else 4
         return P * 4 + V * vb, f"V*{vb} (volume read) + P*4 (ray-sum write)"
@@ -518,7 +518,7 @@ def make_batch_instances(device: str, n: int | None = None, seed: int | None = N
 
 def run_batch_bench(args) -> dict:
     """Config 4: all instances in one batch (one persistent launch per SIRT phase,
-    CUDA graph, BF16 storage) against looping the plain FP32 path over them."""
+    CUDA graph, mixed storage) against looping the plain FP32 path over them."""
     import torch
 
     import mtr
@@ -634,8 +634,8 @@ def serve_rate(mtr, ctx, pool, rate: float, n_req: int, precision: int, rng, kee
 
 
 def run_serve_bench(args) -> dict:
-    """Config 5: rate sweep of the continuous-batching server, mixed (BF16
-    storage) and FP32; the first requests of the lowest rate are compared
+    """Config 5: rate sweep of the continuous-batching server, mixed storage
+    and FP32; the first requests of the lowest rate are compared
     between the two precisions."""
     import torch
 
@@ -758,7 +758,8 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--config", default="c2", choices=sorted(CONFIGS) + ["c4", "c5"])
-    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp16", "fp32"])
+    ap.add_argument("--precision", default="fp16", choices=["bf16", "fp16", "fp32"],
+                    help="mixed storage of the forward copy (fp16: FP16, bf16: BF16), or fp32 throughout")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -835,7 +836,7 @@ def main() -> int:
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": cfg["workload"], "precision": args.precision,
                        "storage": f"{args.precision} volume copy for the forward pass, fp16 projections, "
-                                  "fp16 MACE states, fp32 iterate/residual/weight sums/consensus"
+                                  "fp16 MACE-state deviations from the consensus, fp32 iterate/residual/weight sums/consensus"
                                   if args.precision != "fp32"
                        else "fp32", "voxel_updates_per_step": r["vu"], "parallelism": f"replicas x{world}",
                        "l2": l2_note(cfg),

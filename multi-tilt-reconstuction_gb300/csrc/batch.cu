@@ -267,7 +267,7 @@ mtr_status build_mace_table(mtr_batch* b) {
   for (mtr_recon* r : b->rec) {
     MaceBatchDesc md{};
     md.K = r->K;
-    md.w_half = ck != 0;  // mixed precision keeps the MACE states in FP16
+    md.w_half = ck != 0;  // mixed precision keeps the MACE states as FP16 deviations
     for (int k = 0; k < r->K; ++k) {
       md.w[k] = r->ax[k].w.p;
       md.x[k] = r->ax[k].x.as<float>();

@@ -34,11 +34,31 @@ __global__ void initial_z_kernel(const float* __restrict__ w, const float* __res
     z[i] = __fsub_rn(2.f * wavg[i], w[i]);
 }
 
-// The same from an FP16 state (mixed precision).
-__global__ void initial_z_half_kernel(const __half* __restrict__ w, const float* __restrict__ wavg,
+// Mixed precision stores each MACE state as its FP16 deviation from the FP32
+// consensus, d_k = w_k - w_avg: the axes' states differ from their consensus
+// by much less than they differ from zero, so FP16 rounds d_k far more finely
+// than it would round w_k.  The state's value is w_avg + d_k (one FP32 add).
+__device__ __forceinline__ float state_of(float wavg, __half d) { return __fadd_rn(wavg, __half2float(d)); }
+
+// z = 2*w_avg - w from a deviation state, w = w_avg + d.
+__global__ void initial_z_half_kernel(const __half* __restrict__ d, const float* __restrict__ wavg,
                                       float* __restrict__ z, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float wa = wavg[i];
+    z[i] = __fsub_rn(2.f * wa, state_of(wa, d[i]));
+  }
+}
+
+// d = fp16(w - w_avg) and w = w_avg + d (state to and from its stored form).
+__global__ void state_dev_kernel(const float* __restrict__ w, const float* __restrict__ wavg, __half* __restrict__ d,
+                                 long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    z[i] = __fsub_rn(2.f * wavg[i], __half2float(w[i]));
+    d[i] = __float2half_rn(__fsub_rn(w[i], wavg[i]));
+}
+__global__ void state_value_kernel(const __half* __restrict__ d, const float* __restrict__ wavg, float* __restrict__ w,
+                                   long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    w[i] = state_of(wavg[i], d[i]);
 }
 
 // w = step*(2v - z) + (1-step)*w, with the reference host loop's float
@@ -77,12 +97,14 @@ __global__ void widen_kernel(const __half* __restrict__ src, float* __restrict__
 //   wavg = (sum_k w[k]) / K      (summed in FP64)
 //   x[k] = 2 wavg - w[k]         (the next outer iteration's z_k)
 // and, when copy_kind != 0, x_copy[k] = x[k] in bf16/f16 for the forward pass.
-// With WH (mixed precision) the states w[k] are stored as FP16: each new w_k
-// is rounded to FP16 once when stored, and the next z_k uses the stored value
-// (the next step recomputes z_k from it); the consensus averages the unrounded
-// FP32 states, so the output carries no rounding of the step that made it.  REC: dchange (2 doubles) accumulates
-// sum (wavg_new - wavg_old)^2 and sum wavg_new^2 in FP64, the convergence
-// test's relative change (without it those FP64 operations are not run).
+// With WH (mixed precision) w[k] holds the FP16 deviation d_k = w_k - w_avg
+// (state_of): the new states are computed in FP32, the consensus averages
+// them unrounded (so the output carries no rounding of the step that made
+// it), then each is stored as fp16(w_k - w_avg_new) and the next z_k is formed
+// from the stored value, exactly as the next step recomputes it.  REC: dchange
+// (2 doubles) accumulates sum (wavg_new - wavg_old)^2 and sum wavg_new^2 in
+// FP64, the convergence test's relative change (without it those FP64
+// operations are not run).
 constexpr int kMaxK = MTR_MAX_AXES;
 struct MacePtrs {
   void* w[kMaxK];
@@ -90,18 +112,20 @@ struct MacePtrs {
   void* xc[kMaxK];
 };
 
+// The state w_k at voxel i (consensus wa at that voxel).
 template <bool WH>
-__device__ __forceinline__ float ld_state(const void* w, long long i) {
-  if constexpr (WH) return __half2float(static_cast<const __half*>(w)[i]);
+__device__ __forceinline__ float ld_state(const void* w, long long i, float wa) {
+  if constexpr (WH) return state_of(wa, static_cast<const __half*>(w)[i]);
   else return static_cast<const float*>(w)[i];
 }
-// Stores the new state and returns the value stored.
+// Stores the new state v against the new consensus na and returns the state
+// as it will be read back.
 template <bool WH>
-__device__ __forceinline__ float st_state(void* w, long long i, float v) {
+__device__ __forceinline__ float st_state(void* w, long long i, float v, float na) {
   if constexpr (WH) {
-    const __half h = __float2half_rn(v);
+    const __half h = __float2half_rn(__fsub_rn(v, na));
     static_cast<__half*>(w)[i] = h;
-    return __half2float(h);
+    return state_of(na, h);
   } else {
     static_cast<float*>(w)[i] = v;
     return v;
@@ -121,11 +145,10 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
 #pragma unroll
     for (int k = 0; k < kMaxK; ++k) {
       if (k < K) {
-        const float wk = ld_state<WH>(P.w[k], i);
+        const float wk = ld_state<WH>(P.w[k], i, wa);
         const float zk = __fsub_rn(2.f * wa, wk);
-        const float wu = mann(P.x[k][i], zk, wk, rho);
-        wn[k] = st_state<WH>(P.w[k], i, wu);
-        sum += (double)wu;
+        wn[k] = mann(P.x[k][i], zk, wk, rho);
+        sum += (double)wn[k];
       }
     }
     const float na = (float)(sum * inv_k);  // FP64 mean; the reciprocal spares an FP64 division
@@ -138,7 +161,7 @@ mace_kernel(int K, MacePtrs P, float* __restrict__ wavg, long long n, float rho,
 #pragma unroll
     for (int k = 0; k < kMaxK; ++k) {
       if (k < K) {
-        const float zn = __fsub_rn(2.f * na, wn[k]);
+        const float zn = __fsub_rn(2.f * na, st_state<WH>(P.w[k], i, wn[k], na));
         P.x[k][i] = zn;
         if (copy_kind == 1) static_cast<__nv_bfloat16*>(P.xc[k])[i] = __float2bfloat16_rn(zn);
         else if (copy_kind == 2) static_cast<__half*>(P.xc[k])[i] = __float2half_rn(zn);
@@ -187,10 +210,9 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __re
 #pragma unroll
       for (int k = 0; k < kMaxK; ++k) {
         if (k < K) {
-          const float wk = D.w_half ? ld_state<true>(D.w[k], i) : ld_state<false>(D.w[k], i);
-          const float wu = mann(D.x[k][i], __fsub_rn(2.f * wa, wk), wk, D.rho);
-          wn[k] = D.w_half ? st_state<true>(D.w[k], i, wu) : st_state<false>(D.w[k], i, wu);
-          sum += (double)wu;
+          const float wk = D.w_half ? ld_state<true>(D.w[k], i, wa) : ld_state<false>(D.w[k], i, wa);
+          wn[k] = mann(D.x[k][i], __fsub_rn(2.f * wa, wk), wk, D.rho);
+          sum += (double)wn[k];
         }
       }
       const float na = (float)(sum * inv_k);  // FP64 mean; the reciprocal spares an FP64 division
@@ -198,7 +220,8 @@ mace_batch_kernel(const MaceBatchDesc* __restrict__ descs, const long long* __re
 #pragma unroll
       for (int k = 0; k < kMaxK; ++k) {
         if (k < K) {
-          const float zn = __fsub_rn(2.f * na, wn[k]);
+          const float ws = D.w_half ? st_state<true>(D.w[k], i, wn[k], na) : st_state<false>(D.w[k], i, wn[k], na);
+          const float zn = __fsub_rn(2.f * na, ws);
           D.x[k][i] = zn;
           if (D.copy_kind == 1) static_cast<__nv_bfloat16*>(D.xc[k])[i] = __float2bfloat16_rn(zn);
           else if (D.copy_kind == 2) static_cast<__half*>(D.xc[k])[i] = __float2half_rn(zn);
@@ -245,8 +268,14 @@ void launch_axpy_acc(float* dst, const float* src, long long n, cudaStream_t st)
 void launch_initial_z(const float* w, const float* wavg, float* z, long long n, cudaStream_t st) {
   initial_z_kernel<<<grid_for(n), kThreads, 0, st>>>(w, wavg, z, n);
 }
-void launch_initial_z_half(const __half* w, const float* wavg, float* z, long long n, cudaStream_t st) {
-  initial_z_half_kernel<<<grid_for(n), kThreads, 0, st>>>(w, wavg, z, n);
+void launch_initial_z_half(const __half* d, const float* wavg, float* z, long long n, cudaStream_t st) {
+  initial_z_half_kernel<<<grid_for(n), kThreads, 0, st>>>(d, wavg, z, n);
+}
+void launch_state_dev(const float* w, const float* wavg, __half* d, long long n, cudaStream_t st) {
+  state_dev_kernel<<<grid_for(n), kThreads, 0, st>>>(w, wavg, d, n);
+}
+void launch_state_value(const __half* d, const float* wavg, float* w, long long n, cudaStream_t st) {
+  state_value_kernel<<<grid_for(n), kThreads, 0, st>>>(d, wavg, w, n);
 }
 void launch_update_w(const float* v, const float* z, float* w, long long n, float step, cudaStream_t st) {
   update_w_kernel<<<grid_for(n), kThreads, 0, st>>>(v, z, w, n, step);

@@ -207,7 +207,7 @@ struct ResBatchDesc {
 };
 struct MaceBatchDesc {
   int K;
-  void* w[MTR_MAX_AXES];  // MACE states: FP32, or FP16 when w_half
+  void* w[MTR_MAX_AXES];  // MACE states: FP32, or FP16 deviations from wavg when w_half
   int w_half;
   float* x[MTR_MAX_AXES];
   void* xc[MTR_MAX_AXES];
@@ -253,11 +253,16 @@ int device_sm_count();
 void launch_fill(float* p, long long n, float v, cudaStream_t st);
 void launch_axpy_acc(float* dst, const float* src, long long n, cudaStream_t st);  // dst += src
 // Fused MACE step over K axes (see mace.cu).  w: the K states, FP32 or
-// (w_half) FP16; dchange null: no convergence record.
+// (w_half) FP16 deviations from wavg; dchange null: no convergence record.
 void launch_mace(int K, void* const* w, int w_half, float* const* x, float* wavg, long long n, float rho,
                  void* const* x_copy, int copy_kind, double* dchange, cudaStream_t st);
 void launch_initial_z(const float* w, const float* wavg, float* z, long long n, cudaStream_t st);
-void launch_initial_z_half(const __half* w, const float* wavg, float* z, long long n, cudaStream_t st);
+// Mixed precision keeps each MACE state as the FP16 deviation d = w - w_avg
+// from the FP32 consensus.  z = 2 w_avg - (w_avg + d):
+void launch_initial_z_half(const __half* d, const float* wavg, float* z, long long n, cudaStream_t st);
+// d = fp16(w - w_avg), and back: w = w_avg + d
+void launch_state_dev(const float* w, const float* wavg, __half* d, long long n, cudaStream_t st);
+void launch_state_value(const __half* d, const float* wavg, float* w, long long n, cudaStream_t st);
 void launch_update_w(const float* v, const float* z, float* w, long long n, float step, cudaStream_t st);
 void launch_convert_copy(const float* src, void* dst, int copy_kind, long long n, cudaStream_t st);
 // dst[i] = (float)src[i]: FP16 projections widened for the FP32 WBP kernel.

@@ -45,9 +45,10 @@ long long residual_bytes(int PX, int PY, int A) {
   return std::max((long long)projection_pitch(PX) * PY * A * 4, (long long)pair_pitch(PX) * PY * A * 8);
 }
 
-// Bytes per voxel of an axis' MACE state w_k: FP32, or FP16 in mixed
-// precision (it changes once per outer iteration; the SIRT iterate x_k, which
-// accumulates an update every iteration, stays FP32).
+// Bytes per voxel of an axis' MACE state w_k: FP32, or in mixed precision its
+// FP16 deviation from the FP32 consensus (it changes once per outer
+// iteration; the SIRT iterate x_k, which accumulates an update every
+// iteration, stays FP32).
 long long state_bytes(int precision) { return mixed(precision) ? 2 : 4; }
 
 long long axis_bytes(long long np, long long r_bytes, long long nv, int precision) {
@@ -63,14 +64,26 @@ long long axis_bytes(long long np, long long r_bytes, long long nv, int precisio
   return b;
 }
 
-// w_k = v (FP32 on the device): copied, or rounded to FP16 in mixed precision.
+// w_k = v (FP32 on the device): copied, or in mixed precision stored as
+// fp16(v - w_avg) against the consensus already in r->wavg.
 mtr_status set_state(mtr_recon* r, AxisState& a, const float* v, cudaStream_t st) {
   if (!mixed(r->p.precision)) {
     MTR_CK(r->ctx, cudaMemcpyAsync(a.w.p, v, (size_t)r->nv * 4, cudaMemcpyDefault, st));
     return MTR_OK;
   }
-  launch_convert_copy(v, a.w.p, 2, r->nv, st);
+  launch_state_dev(v, r->wavg.as<float>(), a.w.as<__half>(), r->nv, st);
   MTR_CK_LAUNCH(r->ctx, "state copy");
+  return MTR_OK;
+}
+
+// FP32 value of axis k's state into `out` (device or mapped memory).
+mtr_status state_value(mtr_recon* r, int k, float* out, cudaStream_t st) {
+  if (!mixed(r->p.precision)) {
+    MTR_CK(r->ctx, cudaMemcpyAsync(out, r->ax[k].w.p, (size_t)r->nv * 4, cudaMemcpyDefault, st));
+    return MTR_OK;
+  }
+  launch_state_value(r->ax[k].w.as<__half>(), r->wavg.as<float>(), out, r->nv, st);
+  MTR_CK_LAUNCH(r->ctx, "state value");
   return MTR_OK;
 }
 
@@ -265,17 +278,15 @@ mtr_status mtr::recon_enqueue_init(mtr_recon* r) {
     launch_axpy_acc(wavg, a.x.as<float>(), nv, ctx->stream);
     MTR_CK_LAUNCH(ctx, "initial model sum");
   }
-  // w_k = w_avg; first z_k = 2 w_avg - w_k (= w_avg, up to the FP16 rounding
-  // of a mixed-precision state).
+  // w_k = w_avg (in mixed precision a zero deviation); first z_k = 2 w_avg - w_k = w_avg.
   for (auto& a : r->ax) {
-    mtr_status s = set_state(r, a, wavg, ctx->stream);
-    if (s != MTR_OK) return s;
     if (mixed(r->p.precision)) {
-      launch_initial_z_half(a.w.as<__half>(), wavg, a.x.as<float>(), nv, ctx->stream);
-      MTR_CK_LAUNCH(ctx, "initial z");
+      MTR_CK(ctx, cudaMemsetAsync(a.w.p, 0, (size_t)nv * 2, ctx->stream));
     } else {
-      MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDefault, ctx->stream));
+      mtr_status s = set_state(r, a, wavg, ctx->stream);
+      if (s != MTR_OK) return s;
     }
+    MTR_CK(ctx, cudaMemcpyAsync(a.x.p, wavg, vbytes, cudaMemcpyDefault, ctx->stream));
     if (ck) {
       ProfScope ps(ctx, MTR_KERNEL_OTHER);
       launch_convert_copy(a.x.as<float>(), a.xcopy.p, ck, nv, ctx->stream);
@@ -592,7 +603,7 @@ mtr_status mtr_recon_save(mtr_recon* r, const char* path) {
   h.Z = r->vs.Z;
   h.outer_done = r->outer_done;
   h.precision = r->p.precision;
-  DevBuf tmp;  // FP32 view of an FP16 state (mixed precision)
+  DevBuf tmp;  // FP32 value of an FP16 deviation state (mixed precision)
   if (mixed(r->p.precision)) MTR_CK(ctx, tmp.alloc_pooled(vb, ctx));
   FILE* f = std::fopen(path, "wb");
   if (!f) return set_error(ctx, MTR_ERR_IO, std::string("cannot create ") + path);
@@ -600,7 +611,11 @@ mtr_status mtr_recon_save(mtr_recon* r, const char* path) {
   for (int k = -1; ok && k < r->K; ++k) {
     const void* src = k < 0 ? r->wavg.p : r->ax[k].w.p;
     if (k >= 0 && tmp.p) {  // the file holds FP32 states in every precision
-      launch_widen(r->ax[k].w.as<__half>(), tmp.as<float>(), r->nv, ctx->stream);
+      const mtr_status ss = state_value(r, k, tmp.as<float>(), ctx->stream);
+      if (ss != MTR_OK) {
+        std::fclose(f);
+        return ss;
+      }
       src = tmp.p;
     }
     cudaError_t e = cudaMemcpyAsync(host.data(), src, vb, cudaMemcpyDefault, ctx->stream);
@@ -758,17 +773,17 @@ mtr_status mtr_recon_download_axes(mtr_recon* r, float* out, int mem_kind) {
   if (!mixed(r->p.precision)) {
     for (int k = 0; k < r->K; ++k)
       MTR_CK(ctx, cudaMemcpyAsync(out + (size_t)k * r->nv, r->ax[k].w.p, (size_t)r->nv * 4, kind, ctx->stream));
-  } else if (mem_kind == MTR_MEM_DEVICE) {  // FP16 states widened straight into the caller's array
+  } else if (mem_kind == MTR_MEM_DEVICE) {  // FP32 values of the FP16 deviations straight into the caller's array
     for (int k = 0; k < r->K; ++k) {
-      launch_widen(r->ax[k].w.as<__half>(), out + (size_t)k * r->nv, r->nv, ctx->stream);
-      MTR_CK_LAUNCH(ctx, "widen state");
+      const mtr_status s = state_value(r, k, out + (size_t)k * r->nv, ctx->stream);
+      if (s != MTR_OK) return s;
     }
   } else {
     DevBuf tmp;
     MTR_CK(ctx, tmp.alloc_pooled((size_t)r->nv * 4, ctx));
     for (int k = 0; k < r->K; ++k) {
-      launch_widen(r->ax[k].w.as<__half>(), tmp.as<float>(), r->nv, ctx->stream);
-      MTR_CK_LAUNCH(ctx, "widen state");
+      const mtr_status s = state_value(r, k, tmp.as<float>(), ctx->stream);
+      if (s != MTR_OK) return s;
       MTR_CK(ctx, cudaMemcpyAsync(out + (size_t)k * r->nv, tmp.p, (size_t)r->nv * 4, kind, ctx->stream));
     }
     MTR_CK(ctx, cudaStreamSynchronize(ctx->stream));

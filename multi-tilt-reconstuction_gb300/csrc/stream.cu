@@ -248,17 +248,14 @@ mtr_status mtr::stream_enqueue_init(mtr_recon* r) {
         MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].w, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
         MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].x, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
       }
-    } else {  // w_k = w_avg in FP16, x_k = 2 w_avg - w_k, and the forward copies
-      launch_convert_copy(S.acc.as<float>(), S.xc[0].p, 2, R.n, c);
-      MTR_CK_LAUNCH(ctx, "state copy (streamed)");
-      launch_initial_z_half(S.xc[0].as<__half>(), S.acc.as<float>(), S.x[0].as<float>(), R.n, c);
-      MTR_CK_LAUNCH(ctx, "initial z (streamed)");
+    } else {  // w_k = w_avg (a zero FP16 deviation), x_k = w_avg, and the forward copies
+      MTR_CK(ctx, cudaMemsetAsync(S.xc[0].p, 0, (size_t)R.n * 2, c));
       for (int k = 0; k < K; ++k) {
         MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].w, R.off, 2), S.xc[0].p, (size_t)R.n * 2, cudaMemcpyDefault,
                                     c));
-        MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].x, R.off, 4), S.x[0].p, nb, cudaMemcpyDefault, c));
+        MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].x, R.off, 4), S.acc.p, nb, cudaMemcpyDefault, c));
       }
-      launch_convert_copy(S.x[0].as<float>(), S.xc[0].p, ck, R.n, c);
+      launch_convert_copy(S.acc.as<float>(), S.xc[0].p, ck, R.n, c);
       MTR_CK_LAUNCH(ctx, "volume copy (streamed)");
       for (int k = 0; k < K; ++k)
         MTR_CK(ctx, cudaMemcpyAsync(bytes_at(r->ax[k].xcopy, R.off, 2), S.xc[0].p, (size_t)R.n * 2,

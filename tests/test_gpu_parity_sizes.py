@@ -79,11 +79,14 @@ def test_benchmark_geometry_parity(ctx, name):
     oracle.set_threads(os.cpu_count() or 1)
     p32 = mtr.params(iter_times=no, sirt_inner=ni, sirt_step=lam, mace_step=rho)
     pmx = mtr.params(iter_times=no, sirt_inner=ni, sirt_step=lam, mace_step=rho, precision=mtr.PREC_MIXED_BF16)
+    pmh = mtr.params(iter_times=no, sirt_inner=ni, sirt_step=lam, mace_step=rho, precision=mtr.PREC_MIXED_FP16)
     got32 = ctx.reconstruct(axes, vol, p32)
     gotmx = ctx.reconstruct(axes, vol, pmx)
+    gotmh = ctx.reconstruct(axes, vol, pmh)
     want = oracle.reconstruct(oracle.REF_FAITHFUL, axes, vol, no, ni, lam, rho)
     want64 = oracle.reconstruct(oracle.FP64, axes, vol, no, ni, lam, rho)
     errs = {"fp32_vs_oracle": rel_l2(got32, want), "mixed_bf16_vs_fp64_oracle": rel_l2(gotmx, want64),
+            "mixed_fp16_vs_fp64_oracle": rel_l2(gotmh, want64),
             "fp32_vs_fp64_oracle": rel_l2(got32, want64), "oracle_vs_fp64_oracle": rel_l2(want, want64),
             "volume": list(vol.astuple()), "detector_px": spec["px"], "tilts": len(range(*spec["tilts"])),
             "axes_deg": list(spec["phis"])}
@@ -92,5 +95,6 @@ def test_benchmark_geometry_parity(ctx, name):
     _record(name, errs)
     assert errs["fp32_vs_oracle"] < FP32_TOL
     assert errs["mixed_bf16_vs_fp64_oracle"] < MIXED_TOL
+    assert errs["mixed_fp16_vs_fp64_oracle"] < MIXED_TOL
     if "fp32_vs_reference_kernels" in errs:
         assert errs["fp32_vs_reference_kernels"] < FP32_TOL
