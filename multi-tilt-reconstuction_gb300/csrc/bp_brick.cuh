@@ -146,6 +146,33 @@ __device__ __forceinline__ void bp_column(float (&s)[NZ], const float2* row0, in
   }
 }
 
+// The same from planar pair windows: a detector row's values, then its
+// differences, WX floats each, so a voxel's row r reads p[0] and p[WX] and
+// row r + 1 reads p[2 WX] and p[3 WX] (four 4-byte loads, two FFMAs).
+template <bool ASC, int NZ>
+__device__ __forceinline__ void bp_column_planar(float (&s)[NZ], const float* row0, int WX, float xr, float a3,
+                                                 int lxm, float wy0, float wy1) {
+  constexpr int zf = ASC ? 0 : NZ - 1;
+  const float x = fmaf(a3, (float)zf, xr);
+  const float flx = floorf(x);
+  float fx = x - flx;
+  const float step = fabsf(a3);
+  const float* p = row0 + (magic_int(flx) + lxm);
+  const int w2 = 2 * WX, w3 = 3 * WX;
+#pragma unroll
+  for (int i = 0; i < NZ; ++i) {
+    const int z = ASC ? i : NZ - 1 - i;
+    if (i > 0) {
+      fx += step;
+      const bool adv = fx >= 1.f;
+      fx = adv ? fx - 1.f : fx;
+      p += adv ? 1 : 0;
+    }
+    s[z] = fmaf(wy0, fmaf(fx, p[WX], p[0]), s[z]);
+    s[z] = fmaf(wy1, fmaf(fx, p[w3], p[w2]), s[z]);
+  }
+}
+
 template <bool ASC, int NZ>
 __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float2* b, float xr, float a3, int lxm) {
   constexpr int zf = ASC ? 0 : NZ - 1;
@@ -174,8 +201,9 @@ __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float2* 
 // taps of a line fall on a diagonal of the window that maps several lanes to
 // one shared-memory bank; a patch keeps them compact).  `smem` is the CTA's
 // dynamic shared memory; `reinit` re-initialises the mbarriers of a CTA that
-// already ran a brick.
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ>
+// already ran a brick.  PLANAR (with PAIR): the pair windows hold each
+// detector row as two FP32 rows, its values and then its differences.
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, bool PLANAR = false>
 __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& P, int bx, int by, int bz,
                                          unsigned char* smem, bool reinit) {
   constexpr int BX = LANES == 1 ? kConsumerWarps : 32;
@@ -184,14 +212,15 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   // per pixel, from a pair array whose column c is pixel c - 1; the WBP's
   // windows hold the projections.
   static_assert(!PAIR || MODE == 1, "residual pairs feed the SIRT update only");
-  using WT = typename std::conditional<PAIR, float2, PT>::type;     // window element
+  static_assert(!PLANAR || (PAIR && BZ0), "planar windows are a pair format, for y-maps without a Z term");
+  using WT = typename std::conditional<PLANAR, float, typename std::conditional<PAIR, float2, PT>::type>::type;
   using BT = typename std::conditional<PAIR, float2, float>::type;  // blended-row element
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + NST;
   WinConst* kc = reinterpret_cast<WinConst*>(smem + 128);
   const int A = P.ax.A;
   const size_t kc_bytes = ((size_t)A * sizeof(WinConst) + 127) & ~(size_t)127;
-  const int win_elems = P.WX * P.WY;
+  const int win_elems = P.WX * P.WY * (PLANAR ? 2 : 1);
   const size_t stage_bytes = (((size_t)win_elems * sizeof(WT)) + 127) & ~(size_t)127;
   WT* win0 = reinterpret_cast<WT*>(smem + 128 + kc_bytes);
   // per-warp blended row (uniform-row angles)
@@ -257,8 +286,10 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
         }
         WT* dst = reinterpret_cast<WT*>(reinterpret_cast<unsigned char*>(win0) + s * stage_bytes);
         mbar_arrive_expect_tx(&full[s], bytes);
-        // pair arrays are mapped as FP32 pairs: x = 2 * (first pair column), a multiple of 4
-        tma_load_3d(dst, tmap, PAIR ? 2 * (kc[a].ox + 1) : kc[a].ox, kc[a].oy, a, &full[s]);
+        // interleaved pair arrays are mapped as FP32 pairs: x = 2 * (first pair
+        // column), a multiple of 4; planar ones as two FP32 rows per detector row
+        tma_load_3d(dst, tmap, PLANAR ? kc[a].ox + 1 : PAIR ? 2 * (kc[a].ox + 1) : kc[a].ox,
+                    PLANAR ? 2 * kc[a].oy : kc[a].oy, a, &full[s]);
         issued = a + 1;
       }
       // Drain: the last load issued into each stage must land before exit
@@ -306,9 +337,12 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
       const float fy = yr - fly;
       const int rowi = magic_int(fly) + k.lym;
       if ((unsigned)rowi < lim_y) {
-        const WT* row0 = w + rowi * WX;
+        const WT* row0 = w + rowi * WX * (PLANAR ? 2 : 1);
         for (int i = lane; i < WX; i += 32) {
-          if constexpr (PAIR) {
+          if constexpr (PLANAR) {
+            const float v0 = row0[i], d0 = row0[i + WX], v1 = row0[i + 2 * WX], d1 = row0[i + 3 * WX];
+            blend[i] = make_float2(fmaf(fy, v1 - v0, v0), fmaf(fy, d1 - d0, d0));
+          } else if constexpr (PAIR) {
             const float2 q0 = row0[i], q1 = row0[i + WX];
             blend[i] = make_float2(fmaf(fy, q1.x - q0.x, q0.x), fmaf(fy, q1.y - q0.y, q0.y));
           } else {
@@ -342,6 +376,10 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
         if (blended) {
           if (k.a3 >= 0.f) bp_column_blended<true, NZ>(s, blend, xr, k.a3, k.lxm);
           else bp_column_blended<false, NZ>(s, blend, xr, k.a3, k.lxm);
+        } else if constexpr (PLANAR) {
+          const float* row0 = w + rowi * 2 * WX;
+          if (k.a3 >= 0.f) bp_column_planar<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+          else bp_column_planar<false, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
         } else {
           const WT* row0 = w + rowi * WX;
           if (k.a3 >= 0.f) bp_column<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
@@ -388,9 +426,12 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
         const float fx = x - flx;
         const int ix = magic_int(flx) + k.lxm;
         if ((unsigned)ix >= lim_x) bad = true;
-        const int i0 = bad ? 0 : ix + rowi * WX;  // never index outside the window
+        const int i0 = bad ? 0 : ix + rowi * WX * (PLANAR ? 2 : 1);  // never index outside the window
         float r0, r1;
-        if constexpr (PAIR) {
+        if constexpr (PLANAR) {
+          r0 = fmaf(fx, w[i0 + WX], w[i0]);
+          r1 = fmaf(fx, w[i0 + 3 * WX], w[i0 + 2 * WX]);
+        } else if constexpr (PAIR) {
           const float2 q0 = w[i0], q1 = w[i0 + WX];
           r0 = fmaf(fx, q0.y, q0.x);
           r1 = fmaf(fx, q1.y, q1.x);
@@ -448,17 +489,17 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 // One CTA per brick of one axis.  The grid runs x fastest, then z, then y:
 // bricks of the same rows at all depths run together, so the detector rows
 // they read stay in L2 instead of being re-read from DRAM once per z layer.
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ>
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, bool PLANAR = false>
 // (pair windows take twice the shared memory: 4 CTAs per SM below depth 32)
 __global__ void __launch_bounds__(kThreads, MODE == 1 ? (NZ >= 32 ? 3 : (PAIR ? 4 : 5)) : 4)
 bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
-  bp_brick<PT, MODE, PAIR, LANES, BZ0, NZ>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
+  bp_brick<PT, MODE, PAIR, LANES, BZ0, NZ, PLANAR>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
 }
 
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ>
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, bool PLANAR = false>
 cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cudaStream_t st) {
-  auto kern = bp_tma_kernel<PT, MODE, PAIR, LANES, BZ0, NZ>;
+  auto kern = bp_tma_kernel<PT, MODE, PAIR, LANES, BZ0, NZ, PLANAR>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int BX = LANES == 1 ? kConsumerWarps : 32, BY = LANES == 1 ? 32 : kConsumerWarps;
@@ -469,17 +510,17 @@ cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cud
   return le;
 }
 
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0>
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, bool PLANAR = false>
 cudaError_t launch_nz(const CUtensorMap& map, const BpArgs& P, const BpPlan& plan, cudaStream_t st) {
   // WBP: depth 16 or 8 (it runs once per reconstruction).  SIRT: the tuned depth.
   if constexpr (MODE == 0) {
     if (plan.nz == 16) return launch_one<PT, 0, PAIR, LANES, BZ0, 16>(map, P, plan.smem, st);
     return launch_one<PT, 0, PAIR, LANES, BZ0, 8>(map, P, plan.smem, st);
   } else {
-    if (plan.nz == 8) return launch_one<PT, MODE, PAIR, LANES, BZ0, 8>(map, P, plan.smem, st);
-    if (plan.nz == 4) return launch_one<PT, MODE, PAIR, LANES, BZ0, 4>(map, P, plan.smem, st);
-    if (plan.nz == 16) return launch_one<PT, MODE, PAIR, LANES, BZ0, 16>(map, P, plan.smem, st);
-    if (plan.nz == 32) return launch_one<PT, MODE, PAIR, LANES, BZ0, 32>(map, P, plan.smem, st);
+    if (plan.nz == 8) return launch_one<PT, MODE, PAIR, LANES, BZ0, 8, PLANAR>(map, P, plan.smem, st);
+    if (plan.nz == 4) return launch_one<PT, MODE, PAIR, LANES, BZ0, 4, PLANAR>(map, P, plan.smem, st);
+    if (plan.nz == 16) return launch_one<PT, MODE, PAIR, LANES, BZ0, 16, PLANAR>(map, P, plan.smem, st);
+    if (plan.nz == 32) return launch_one<PT, MODE, PAIR, LANES, BZ0, 32, PLANAR>(map, P, plan.smem, st);
     return cudaErrorInvalidValue;
   }
 }

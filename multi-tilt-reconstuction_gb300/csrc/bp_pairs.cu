@@ -7,14 +7,23 @@
 // subtraction and an FFMA).  Twice the window bytes: the tuner keeps this
 // layout for an axis only where it measures faster (on lines of lanes that
 // share detector rows it saves a third of the instructions; on oblique axes
-// the 8-byte loads of a warp conflict in the shared-memory banks).  Separate
-// from bp_tma.cu so that the two sets of instantiations compile in parallel.
+// the 8-byte loads of a warp conflict in the shared-memory banks).  Planar
+// pair windows hold a detector row as two FP32 rows, its values and then its
+// differences: four 4-byte loads per voxel, with the FP32 window's bank
+// pattern, but still one FFMA per row.  Separate from bp_tma.cu so that the
+// two sets of instantiations compile in parallel.
 #include "bp_brick.cuh"
 
 namespace mtr {
 
 cudaError_t launch_backproject_tma_pairs(const CUtensorMap& map, const BpPlan& plan, const BpArgs& P,
                                          cudaStream_t st) {
+  if (plan.planar) {  // (planned for y-maps without a Z term only)
+    if (!plan.bz0) return cudaErrorInvalidValue;
+    if (plan.lanes == 2) return launch_nz<float, 1, true, 2, true, true>(map, P, plan, st);
+    if (plan.lanes == 1) return launch_nz<float, 1, true, 1, true, true>(map, P, plan, st);
+    return launch_nz<float, 1, true, 0, true, true>(map, P, plan, st);
+  }
   if (plan.lanes == 2) return plan.bz0 ? launch_nz<float, 1, true, 2, true>(map, P, plan, st)
                                        : launch_nz<float, 1, true, 2, false>(map, P, plan, st);
   if (plan.lanes == 1) return plan.bz0 ? launch_nz<float, 1, true, 1, true>(map, P, plan, st)

@@ -214,15 +214,19 @@ double window_bank_cost(const std::vector<double>& xc, const std::vector<double>
 namespace {
 
 // Window box for a brick of depth nz over all angles of an axis.
-BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool pairs,
+BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vector<double>& yc, int A, int fmt,
                                  int nz, int lane) {
   BpPlan p;
-  // FP32 windows start on a 4-pixel (16-byte) boundary; pair windows on an
-  // even pair column (16 bytes of pairs)
+  // FP32 and planar windows start on a 4-pixel (16-byte) boundary;
+  // interleaved pair windows on an even pair column (16 bytes of pairs)
+  const bool pairs = fmt == 1;
   p.align = pairs ? 2 : 4;
-  p.pairs = pairs;
+  p.pairs = fmt != 0;
+  p.planar = fmt == 2;
   p.nz = nz;
-  const size_t es = pairs ? 8 : 4;  // bytes per window element
+  const size_t es = pairs ? 8 : 4;          // bytes per window element
+  const int planes = p.planar ? 2 : 1;      // window rows per detector row
+  const size_t bes = p.pairs ? 8 : 4;       // bytes per blended-row element
   // Choose the lane axis so that consecutive lanes step along detector x.
   double sx = 0, sy = 0;
   bool bz0 = true;
@@ -247,9 +251,9 @@ BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vecto
   const int wx_min = (wx + p.align - 1) / p.align * p.align;
   p.WY = (int)std::ceil(ey) + 4;
   auto smem_for = [&](int WX) {
-    const size_t stage = (((size_t)WX * p.WY * es) + 127) & ~(size_t)127;
+    const size_t stage = (((size_t)WX * p.WY * planes * es) + 127) & ~(size_t)127;
     return 128 + ((((size_t)A * sizeof(WinConst)) + 127) & ~(size_t)127) + NST * stage +
-           (((size_t)kConsumerWarps * WX * es + 127) & ~(size_t)127);  // per-warp blended rows
+           (((size_t)kConsumerWarps * WX * bes + 127) & ~(size_t)127);  // per-warp blended rows
   };
   // Row pitch (= box width): the smallest one whose tap loads have the fewest
   // bank conflicts, among widths that keep 5 CTAs per SM.  A wider box only
@@ -267,7 +271,9 @@ BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vecto
   for (int WX = wx_min; WX <= std::min(max_wx, wx_min + 16 * p.align); WX += p.align) {
     if (WX > wx_min && smem_for(WX) > (size_t)(228 * 1024 / 5 - 1024)) break;
     if (!known[WX & 31]) {
-      cost_of[WX & 31] = window_bank_cost(xc, yc, A, p.lanes, nz, WX, pairs);
+      // (planar: each of a voxel's four loads is a tap pattern of row pitch 2 WX)
+      cost_of[WX & 31] = p.planar ? window_bank_cost(xc, yc, A, p.lanes, nz, 2 * WX, false)
+                                  : window_bank_cost(xc, yc, A, p.lanes, nz, WX, pairs);
       known[WX & 31] = true;
     }
     const double c = cost_of[WX & 31];
@@ -276,7 +282,8 @@ BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vecto
       p.WX = WX;
     }
   }
-  p.ok = p.WX <= max_wx && p.WY <= 256 && (nz == 4 || nz == 8 || nz == 16 || nz == 32);
+  p.ok = p.WX <= max_wx && p.WY * planes <= 256 && (nz == 4 || nz == 8 || nz == 16 || nz == 32) &&
+         (!p.planar || bz0);  // (planar windows: y-maps without a Z term)
   p.smem = smem_for(p.WX);
   if (p.smem > 227 * 1024) p.ok = false;
   return p;
@@ -286,10 +293,10 @@ PlanMemo<BpPlan> g_bp_plans;
 
 }  // namespace
 
-BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, bool pairs, int nz,
+BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, int fmt, int nz,
                         int lane) {
-  return g_bp_plans.get(plan_key(xc, yc, A, {pairs ? 1 : 0, nz, lane}),
-                        [&] { return plan_backproject_uncached(xc, yc, A, pairs, nz, lane); });
+  return g_bp_plans.get(plan_key(xc, yc, A, {fmt, nz, lane}),
+                        [&] { return plan_backproject_uncached(xc, yc, A, fmt, nz, lane); });
 }
 
 template <typename PT>

@@ -300,9 +300,13 @@ struct AxisState {
 };
 
 // Tensor map over an axis' residual in pair form: FP32 elements, rows of
-// 2 * pitch2 floats, boxes of 2 * WX floats (WX pairs) by WY rows.
+// 2 * pitch2 floats, boxes of 2 * WX floats (WX pairs) by WY rows; planar
+// pairs as 2 * PY rows of pitch2 floats (each detector row's values, then its
+// differences), boxes of WX floats by 2 * WY rows.
 inline bool encode_pair_map(CUtensorMap* m, const AxisState& a, const BpPlan& p) {
-  return p.pairs && encode_tensor_map_3d(m, a.r.p, false, 2 * a.pitch2, 2 * a.pitch2, a.PY, a.A, 2 * p.WX, p.WY);
+  if (!p.pairs) return false;
+  if (p.planar) return encode_tensor_map_3d(m, a.r.p, false, a.pitch2, a.pitch2, 2 * a.PY, a.A, p.WX, 2 * p.WY);
+  return encode_tensor_map_3d(m, a.r.p, false, 2 * a.pitch2, 2 * a.pitch2, a.PY, a.A, 2 * p.WX, p.WY);
 }
 // Tensor map over an axis' residual in the form its SIRT update reads: pairs,
 // or FP32 rows of `pitch` elements.

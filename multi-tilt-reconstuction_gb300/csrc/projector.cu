@@ -284,9 +284,11 @@ residual_kernel(long long n, long long n4, const BT* __restrict__ b, float* __re
 // chunk; r[c-1] of a lane's first column comes from the lane below (lane 0:
 // the last column of the previous chunk).  s is reset to zero.  Returns the
 // lane's sum of r^2.
-template <typename BT>
+// PLANAR: the row's pairs are written as two planes of pitch2 floats, the
+// values and then the differences (out is the row's first float).
+template <typename BT, bool PLANAR>
 __device__ __forceinline__ float residual_pair_row(const BT* __restrict__ br, float* __restrict__ sr,
-                                                   const float* __restrict__ cr, float2* __restrict__ out, int pitch,
+                                                   const float* __restrict__ cr, float* __restrict__ out, int pitch,
                                                    int pitch2, int lane) {
   float carry = 0.f, sq = 0.f;
   for (int c0 = 0; c0 < pitch2; c0 += 128) {
@@ -308,25 +310,31 @@ __device__ __forceinline__ float residual_pair_row(const BT* __restrict__ br, fl
     if (lane == 0) prev = carry;
     carry = __shfl_sync(0xffffffffu, r4[3], 31);
     if (col < pitch2) {  // pitch2 is a multiple of 4: four pairs, 32 bytes
-      float4* o = reinterpret_cast<float4*>(out + col);
-      o[0] = make_float4(prev, r4[0] - prev, r4[0], r4[1] - r4[0]);
-      o[1] = make_float4(r4[1], r4[2] - r4[1], r4[2], r4[3] - r4[2]);
+      if constexpr (PLANAR) {
+        *reinterpret_cast<float4*>(out + col) = make_float4(prev, r4[0], r4[1], r4[2]);
+        *reinterpret_cast<float4*>(out + pitch2 + col) =
+            make_float4(r4[0] - prev, r4[1] - r4[0], r4[2] - r4[1], r4[3] - r4[2]);
+      } else {
+        float4* o = reinterpret_cast<float4*>(out + 2 * col);
+        o[0] = make_float4(prev, r4[0] - prev, r4[0], r4[1] - r4[0]);
+        o[1] = make_float4(r4[1], r4[2] - r4[1], r4[2], r4[3] - r4[2]);
+      }
     }
   }
   return sq;
 }
 
 // One warp per detector row (rows = AngN * PY); FP64 norm when NORM.
-template <typename BT, bool NORM>
+template <typename BT, bool NORM, bool PLANAR>
 __global__ void __launch_bounds__(256)
 residual_pairs_kernel(long long rows, int pitch, int pitch2, const BT* __restrict__ b, float* __restrict__ s,
-                      const float* __restrict__ c, float2* __restrict__ rp, double* __restrict__ norm2) {
+                      const float* __restrict__ c, float* __restrict__ rp, double* __restrict__ norm2) {
   const int lane = threadIdx.x & 31;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   double acc = 0.0;
   for (long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; row < rows; row += nwarps) {
-    const float sq = residual_pair_row(b + row * pitch, s + row * pitch, c + row * pitch, rp + row * pitch2, pitch,
-                                       pitch2, lane);
+    const float sq = residual_pair_row<BT, PLANAR>(b + row * pitch, s + row * pitch, c + row * pitch,
+                                                   rp + row * 2 * pitch2, pitch, pitch2, lane);
     if (NORM) acc += (double)sq;
   }
   if (NORM) {
@@ -408,19 +416,25 @@ void launch_residual_batch(const ResBatchDesc* descs, const long long* first, in
 }
 
 template <typename BT>
-void launch_residual_pairs(long long rows, int pitch, int pitch2, const BT* b, float* s, const float* c, float2* rp,
-                           double* norm2, cudaStream_t st) {
+void launch_residual_pairs(long long rows, int pitch, int pitch2, const BT* b, float* s, const float* c, float* rp,
+                           bool planar, double* norm2, cudaStream_t st) {
   long long blocks = (rows + 7) / 8;  // 8 warps per block, one row per warp
   const long long cap = (long long)device_sm_count() * 16;
   if (blocks > cap) blocks = cap;  // grid-stride over the rest
   if (blocks < 1) blocks = 1;
-  if (norm2) residual_pairs_kernel<BT, true><<<(unsigned)blocks, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
-  else residual_pairs_kernel<BT, false><<<(unsigned)blocks, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
+  const unsigned g = (unsigned)blocks;
+  if (planar) {
+    if (norm2) residual_pairs_kernel<BT, true, true><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
+    else residual_pairs_kernel<BT, false, true><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
+  } else {
+    if (norm2) residual_pairs_kernel<BT, true, false><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
+    else residual_pairs_kernel<BT, false, false><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
+  }
 }
 
-template void launch_residual_pairs<float>(long long, int, int, const float*, float*, const float*, float2*, double*,
-                                           cudaStream_t);
-template void launch_residual_pairs<__half>(long long, int, int, const __half*, float*, const float*, float2*,
+template void launch_residual_pairs<float>(long long, int, int, const float*, float*, const float*, float*, bool,
+                                           double*, cudaStream_t);
+template void launch_residual_pairs<__half>(long long, int, int, const __half*, float*, const float*, float*, bool,
                                             double*, cudaStream_t);
 
 template void launch_backproject<float>(const AxisDev&, const VolDev&, const float*, int, float, float*, float*,

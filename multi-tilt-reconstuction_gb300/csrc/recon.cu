@@ -195,10 +195,10 @@ mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
   if (a.tma && a.plan.pairs) {  // this axis' windowed update reads (value, next - value) pairs
     if (mixed(r->p.precision))
       launch_residual_pairs<__half>(rows, a.pitch, a.pitch2, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(),
-                                    a.r.as<float2>(), norm, ctx->stream);
+                                    a.r.as<float>(), a.plan.planar, norm, ctx->stream);
     else
       launch_residual_pairs<float>(rows, a.pitch, a.pitch2, a.b.as<float>(), a.s.as<float>(), a.cf.as<float>(),
-                                   a.r.as<float2>(), norm, ctx->stream);
+                                   a.r.as<float>(), a.plan.planar, norm, ctx->stream);
   } else if (mixed(r->p.precision)) {
     launch_residual<__half, float>(a.np, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), norm,
                                    ctx->stream);
@@ -537,7 +537,7 @@ mtr_status mtr_recon_create(mtr_context* ctx, int n_axes, const mtr_axis* axes, 
       // The WBP gathers the same windows as the SIRT update: the lane layout
       // tuned for it (lines or 8x4 patches), at depth 16 where the tuned depth
       // is 16 or more, else 8.
-      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, false, a.plan.ok && a.plan.nz >= 16 ? 16 : 8,
+      a.plan_b = plan_backproject(a.hxc, a.hyc, a.A, 0, a.plan.ok && a.plan.nz >= 16 ? 16 : 8,
                                   a.plan.ok ? a.plan.lanes : -1);
       a.tma_b = a.plan_b.ok && encode_tensor_map_3d(&a.map_b, mx ? a.r.p : a.b.p, false, a.PX, a.pitch, a.PY, a.A,
                                                     a.plan_b.WX, a.plan_b.WY);
@@ -853,7 +853,7 @@ mtr_status mtr_recon_describe(const mtr_recon* r, char* buf, int cap) {
                   "\"window_format\":\"%s\"},"
                   "\"forward\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\",\"y_has_z\":%s}}",
                   k ? "," : "", k, a.tma ? "true" : "false", a.plan.nz, a.plan.WX, a.plan.WY,
-                  a.plan.lanes == 1 ? "y" : a.plan.lanes == 2 ? "patch" : "x", a.plan.pairs ? "pairs" : "fp32",
+                  a.plan.lanes == 1 ? "y" : a.plan.lanes == 2 ? "patch" : "x", a.plan.planar ? "planar pairs" : a.plan.pairs ? "pairs" : "fp32",
                   a.ftma ? "true" : "false", a.fplan.nz, a.fplan.WX, a.fplan.WY,
                   a.fplan.lanes == 1 ? "y" : a.fplan.lanes == 2 ? "patch" : "x", a.fplan.bz0 ? "false" : "true");
     s += t;

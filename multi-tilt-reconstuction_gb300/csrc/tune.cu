@@ -13,18 +13,21 @@
 //  * the SIRT back-projection's window format: FP32 residual values, or
 //    (value, next - value) pairs that halve the tap loads but double the
 //    window and load 8 bytes per lane (faster where a warp's lanes share
-//    detector rows, slower where their 8-byte loads conflict in the banks).
-// For each tilt axis the tuner times every candidate (2 formats x depth
+//    detector rows, slower where their 8-byte loads conflict in the banks),
+//    or the same pairs as two FP32 planes per row (4-byte loads with the FP32
+//    window's bank pattern, one FFMA per row).
+// For each tilt axis the tuner times every candidate (3 formats x depth
 // 4/8/16/32 x lines along X / lines along Y / patches for the SIRT
 // back-projection, depth 8/16/32 x the same three layouts for the forward
-// splat) with CUDA events on the reconstruction's own buffers, over at most
-// 32 Z planes, before they hold data (each candidate launch writes only
-// scratch that the run overwrites), and keeps the fastest.  Results are
-// cached per process by a geometry key and, when MTR_AUTOTUNE_CACHE names a
-// file, persisted there as JSON ({"key": [bp_depth, fwd_depth, bp_lane,
-// fwd_lane, bp_pairs], ...}).  MTR_AUTOTUNE=0 disables tuning (depths 8 and
-// 16, lane axis by slope, FP32 windows);
-// MTR_FORCE_DEPTHS=bp,fwd[,bp_lane,fwd_lane[,bp_pairs]] pins the choice.
+// splat) with CUDA events on the reconstruction's own buffers, over a Z-slab
+// of the frame sized for 8 waves of the deepest tile, before they hold data
+// (each candidate launch writes only scratch that the run overwrites), and
+// keeps the fastest.  Results are cached per process by a geometry key and,
+// when MTR_AUTOTUNE_CACHE names a file, persisted there as JSON ({"key":
+// [bp_depth, fwd_depth, bp_lane, fwd_lane, bp_format], ...}; bp_format 0 FP32
+// windows, 1 interleaved pairs, 2 planar pairs).  MTR_AUTOTUNE=0 disables
+// tuning (depths 8 and 16, lane axis by slope, FP32 windows);
+// MTR_FORCE_DEPTHS=bp,fwd[,bp_lane,fwd_lane[,bp_format]] pins the choice.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -45,7 +48,7 @@ namespace {
 
 struct Choice {
   int bp_nz = 8, fwd_nz = 16, bp_lane = -1, fwd_lane = -1;
-  int bp_pairs = 0;  // SIRT update over residual-pair windows (1) or FP32 windows (0)
+  int bp_pairs = 0;  // SIRT update window format: 0 FP32, 1 interleaved residual pairs, 2 planar pairs
 };
 
 std::mutex g_mu;
@@ -106,7 +109,7 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
   }
   char buf[256];
   // the trailing tag names the timing method, so choices cached by an older one are not reused
-  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t7", a.PX, a.PY,
+  std::snprintf(buf, sizeof(buf), "p%dx%dx%d_v%dx%dx%d_m%.2f,%.2f,%.2f,%.2f,%.2f,%.2f_z%d_prec%d_t8", a.PX, a.PY,
                 a.A, v.NX, v.NY, v.NZ, m[0], m[1], m[2], m[3], m[4], m[5], bz0 ? 0 : 1, precision);
   return buf;
 }
@@ -206,12 +209,12 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
     std::vector<BpPlan> bps;
     std::vector<CUtensorMap> bmaps;
     // (the candidates keep pointers into these: no reallocation)
-    bps.reserve(6 * std::size(kBpDepths));
-    bmaps.reserve(6 * std::size(kBpDepths));
-    for (int pairs = 0; pairs < 2; ++pairs)
+    bps.reserve(9 * std::size(kBpDepths));  // 3 formats x 3 lane layouts x the depths
+    bmaps.reserve(9 * std::size(kBpDepths));
+    for (int fmt = 0; fmt < 3; ++fmt)
       for (int lane = 0; lane < 3; ++lane)
         for (int nz : kBpDepths) {
-          BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, pairs != 0, nz, lane);
+          BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, fmt, nz, lane);
           CUtensorMap m;
           if (!p.ok || !encode_residual_map(&m, a, p)) continue;
           bps.push_back(p);
@@ -225,7 +228,7 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
           Choice c;
           c.bp_nz = nz;
           c.bp_lane = lane;
-          c.bp_pairs = pairs;
+          c.bp_pairs = fmt;
           what.push_back(c);
         }
     int k = fastest(ctx->stream, cands);
@@ -277,7 +280,7 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
   }
   // the timing runs wrote into s and the tuner's scratch: restore the zeros
   cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream);
-  a.plan = plan_backproject(a.hxc, a.hyc, a.A, ch.bp_pairs != 0, ch.bp_nz, ch.bp_lane);
+  a.plan = plan_backproject(a.hxc, a.hyc, a.A, std::min(std::max(ch.bp_pairs, 0), 2), ch.bp_nz, ch.bp_lane);
   a.tma = a.plan.ok && encode_residual_map(&a.map_r, a, a.plan);
   a.fplan = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, ch.fwd_nz, ch.fwd_lane);
   a.ftma = a.fplan.ok &&

@@ -193,7 +193,9 @@ def test_windowed_and_plain_kernels_agree(ctx, monkeypatch):
 @pytest.mark.parametrize("depths", ["4,8,0,0", "8,16,1,1", "16,32,0,1", "16,8,1,0", "8,32", "16,16,2,0", "4,8,2,1",
                                     "8,32,0,2", "16,8,2,2", "32,32,0,0", "32,16,2,1", "32,8,1,2",
                                     # the SIRT update over residual-pair windows
-                                    "8,16,0,0,1", "16,32,2,1,1", "32,8,1,2,1", "4,16,2,0,1", "32,32,0,0,1"])
+                                    "8,16,0,0,1", "16,32,2,1,1", "32,8,1,2,1", "4,16,2,0,1", "32,32,0,0,1",
+                                    # ... over planar residual-pair windows
+                                    "16,32,2,0,2", "8,16,0,1,2", "32,8,1,2,2", "4,32,2,2,2"])
 @pytest.mark.parametrize("name", ["mid", "mid_oblique"])
 def test_every_brick_depth_matches_oracle(ctx, monkeypatch, name, depths):
     monkeypatch.setenv("MTR_FORCE_DEPTHS", depths)
@@ -217,7 +219,7 @@ def test_autotune_cache_file(ctx, monkeypatch, tmp_path):
     d = json.loads(cache.read_text())
     # lane -1: no windowed candidate fits that detector (the plain kernel runs)
     assert d and all(b in (4, 8, 16, 32) and f in (8, 16, 32) and bl in (-1, 0, 1, 2) and fl in (-1, 0, 1, 2)
-                     and bp in (0, 1) for b, f, bl, fl, bp in d.values())
+                     and bp in (0, 1, 2) for b, f, bl, fl, bp in d.values())
     key = next(k for k in d if k.startswith("p72x72x13_v64x48x19"))
     assert d[key][2] in (0, 1, 2) and d[key][3] in (0, 1, 2)  # this detector fits both windowed kernels
 
