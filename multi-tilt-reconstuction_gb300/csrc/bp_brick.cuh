@@ -173,6 +173,33 @@ __device__ __forceinline__ void bp_column_planar(float (&s)[NZ], const float* ro
   }
 }
 
+// The same from FP16 pair windows (mixed precision): a detector row's tap
+// pair is one 4-byte load of (value, next - value) in FP16, widened to FP32
+// before the interpolation.  Half the shared-memory bytes of the FP32 formats.
+template <bool ASC, int NZ>
+__device__ __forceinline__ void bp_column_half(float (&s)[NZ], const __half2* row0, int WX, float xr, float a3,
+                                               int lxm, float wy0, float wy1) {
+  constexpr int zf = ASC ? 0 : NZ - 1;
+  const float x = fmaf(a3, (float)zf, xr);
+  const float flx = floorf(x);
+  float fx = x - flx;
+  const float step = fabsf(a3);
+  const __half2* p = row0 + (magic_int(flx) + lxm);
+#pragma unroll
+  for (int i = 0; i < NZ; ++i) {
+    const int z = ASC ? i : NZ - 1 - i;
+    if (i > 0) {
+      fx += step;
+      const bool adv = fx >= 1.f;
+      fx = adv ? fx - 1.f : fx;
+      p += adv ? 1 : 0;
+    }
+    const float2 q0 = __half22float2(p[0]), q1 = __half22float2(p[WX]);
+    s[z] = fmaf(wy0, fmaf(fx, q0.y, q0.x), s[z]);
+    s[z] = fmaf(wy1, fmaf(fx, q1.y, q1.x), s[z]);
+  }
+}
+
 template <bool ASC, int NZ>
 __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float2* b, float xr, float a3, int lxm) {
   constexpr int zf = ASC ? 0 : NZ - 1;
@@ -201,9 +228,10 @@ __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float2* 
 // taps of a line fall on a diagonal of the window that maps several lanes to
 // one shared-memory bank; a patch keeps them compact).  `smem` is the CTA's
 // dynamic shared memory; `reinit` re-initialises the mbarriers of a CTA that
-// already ran a brick.  PLANAR (with PAIR): the pair windows hold each
-// detector row as two FP32 rows, its values and then its differences.
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, bool PLANAR = false>
+// already ran a brick.  PF (pair format, with PAIR): 0 interleaved FP32
+// pairs; 1 planar FP32 pairs, each detector row as two FP32 rows, its values
+// and then its differences; 2 FP16 pairs (value, next - value) in 32 bits.
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, int PF = 0>
 __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& P, int bx, int by, int bz,
                                          unsigned char* smem, bool reinit) {
   constexpr int BX = LANES == 1 ? kConsumerWarps : 32;
@@ -212,8 +240,11 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
   // per pixel, from a pair array whose column c is pixel c - 1; the WBP's
   // windows hold the projections.
   static_assert(!PAIR || MODE == 1, "residual pairs feed the SIRT update only");
-  static_assert(!PLANAR || (PAIR && BZ0), "planar windows are a pair format, for y-maps without a Z term");
-  using WT = typename std::conditional<PLANAR, float, typename std::conditional<PAIR, float2, PT>::type>::type;
+  constexpr bool PLANAR = PAIR && PF == 1, HALF = PAIR && PF == 2;
+  static_assert(!PLANAR || BZ0, "planar windows are a pair format, for y-maps without a Z term");
+  using WT = typename std::conditional<
+      PLANAR, float,
+      typename std::conditional<HALF, __half2, typename std::conditional<PAIR, float2, PT>::type>::type>::type;
   using BT = typename std::conditional<PAIR, float2, float>::type;  // blended-row element
   uint64_t* full = reinterpret_cast<uint64_t*>(smem);
   uint64_t* empty = full + NST;
@@ -288,7 +319,7 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
         mbar_arrive_expect_tx(&full[s], bytes);
         // interleaved pair arrays are mapped as FP32 pairs: x = 2 * (first pair
         // column), a multiple of 4; planar ones as two FP32 rows per detector row
-        tma_load_3d(dst, tmap, PLANAR ? kc[a].ox + 1 : PAIR ? 2 * (kc[a].ox + 1) : kc[a].ox,
+        tma_load_3d(dst, tmap, (PLANAR || HALF) ? kc[a].ox + 1 : PAIR ? 2 * (kc[a].ox + 1) : kc[a].ox,
                     PLANAR ? 2 * kc[a].oy : kc[a].oy, a, &full[s]);
         issued = a + 1;
       }
@@ -342,6 +373,9 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
           if constexpr (PLANAR) {
             const float v0 = row0[i], d0 = row0[i + WX], v1 = row0[i + 2 * WX], d1 = row0[i + 3 * WX];
             blend[i] = make_float2(fmaf(fy, v1 - v0, v0), fmaf(fy, d1 - d0, d0));
+          } else if constexpr (HALF) {
+            const float2 q0 = __half22float2(row0[i]), q1 = __half22float2(row0[i + WX]);
+            blend[i] = make_float2(fmaf(fy, q1.x - q0.x, q0.x), fmaf(fy, q1.y - q0.y, q0.y));
           } else if constexpr (PAIR) {
             const float2 q0 = row0[i], q1 = row0[i + WX];
             blend[i] = make_float2(fmaf(fy, q1.x - q0.x, q0.x), fmaf(fy, q1.y - q0.y, q0.y));
@@ -380,6 +414,10 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
           const float* row0 = w + rowi * 2 * WX;
           if (k.a3 >= 0.f) bp_column_planar<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
           else bp_column_planar<false, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+        } else if constexpr (HALF) {
+          const __half2* row0 = w + rowi * WX;
+          if (k.a3 >= 0.f) bp_column_half<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
+          else bp_column_half<false, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
         } else {
           const WT* row0 = w + rowi * WX;
           if (k.a3 >= 0.f) bp_column<true, NZ>(s, row0, WX, xr, k.a3, k.lxm, 1.f - fy, fy);
@@ -431,6 +469,10 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
         if constexpr (PLANAR) {
           r0 = fmaf(fx, w[i0 + WX], w[i0]);
           r1 = fmaf(fx, w[i0 + 3 * WX], w[i0 + 2 * WX]);
+        } else if constexpr (HALF) {
+          const float2 q0 = __half22float2(w[i0]), q1 = __half22float2(w[i0 + WX]);
+          r0 = fmaf(fx, q0.y, q0.x);
+          r1 = fmaf(fx, q1.y, q1.x);
         } else if constexpr (PAIR) {
           const float2 q0 = w[i0], q1 = w[i0 + WX];
           r0 = fmaf(fx, q0.y, q0.x);
@@ -489,17 +531,17 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 // One CTA per brick of one axis.  The grid runs x fastest, then z, then y:
 // bricks of the same rows at all depths run together, so the detector rows
 // they read stay in L2 instead of being re-read from DRAM once per z layer.
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, bool PLANAR = false>
-// (pair windows take twice the shared memory: 4 CTAs per SM below depth 32)
-__global__ void __launch_bounds__(kThreads, MODE == 1 ? (NZ >= 32 ? 3 : (PAIR ? 4 : 5)) : 4)
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, int PF = 0>
+// (FP32 pair windows take twice the shared memory: 4 CTAs per SM below depth 32)
+__global__ void __launch_bounds__(kThreads, MODE == 1 ? (NZ >= 32 ? 3 : (PAIR && PF != 2 ? 4 : 5)) : 4)
 bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
-  bp_brick<PT, MODE, PAIR, LANES, BZ0, NZ, PLANAR>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
+  bp_brick<PT, MODE, PAIR, LANES, BZ0, NZ, PF>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
 }
 
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, bool PLANAR = false>
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, int PF = 0>
 cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cudaStream_t st) {
-  auto kern = bp_tma_kernel<PT, MODE, PAIR, LANES, BZ0, NZ, PLANAR>;
+  auto kern = bp_tma_kernel<PT, MODE, PAIR, LANES, BZ0, NZ, PF>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   const int BX = LANES == 1 ? kConsumerWarps : 32, BY = LANES == 1 ? 32 : kConsumerWarps;
@@ -510,17 +552,17 @@ cudaError_t launch_one(const CUtensorMap& map, const BpArgs& P, size_t smem, cud
   return le;
 }
 
-template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, bool PLANAR = false>
+template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int PF = 0>
 cudaError_t launch_nz(const CUtensorMap& map, const BpArgs& P, const BpPlan& plan, cudaStream_t st) {
   // WBP: depth 16 or 8 (it runs once per reconstruction).  SIRT: the tuned depth.
   if constexpr (MODE == 0) {
     if (plan.nz == 16) return launch_one<PT, 0, PAIR, LANES, BZ0, 16>(map, P, plan.smem, st);
     return launch_one<PT, 0, PAIR, LANES, BZ0, 8>(map, P, plan.smem, st);
   } else {
-    if (plan.nz == 8) return launch_one<PT, MODE, PAIR, LANES, BZ0, 8, PLANAR>(map, P, plan.smem, st);
-    if (plan.nz == 4) return launch_one<PT, MODE, PAIR, LANES, BZ0, 4, PLANAR>(map, P, plan.smem, st);
-    if (plan.nz == 16) return launch_one<PT, MODE, PAIR, LANES, BZ0, 16, PLANAR>(map, P, plan.smem, st);
-    if (plan.nz == 32) return launch_one<PT, MODE, PAIR, LANES, BZ0, 32, PLANAR>(map, P, plan.smem, st);
+    if (plan.nz == 8) return launch_one<PT, MODE, PAIR, LANES, BZ0, 8, PF>(map, P, plan.smem, st);
+    if (plan.nz == 4) return launch_one<PT, MODE, PAIR, LANES, BZ0, 4, PF>(map, P, plan.smem, st);
+    if (plan.nz == 16) return launch_one<PT, MODE, PAIR, LANES, BZ0, 16, PF>(map, P, plan.smem, st);
+    if (plan.nz == 32) return launch_one<PT, MODE, PAIR, LANES, BZ0, 32, PF>(map, P, plan.smem, st);
     return cudaErrorInvalidValue;
   }
 }

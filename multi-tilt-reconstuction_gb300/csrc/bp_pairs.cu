@@ -10,7 +10,9 @@
 // the 8-byte loads of a warp conflict in the shared-memory banks).  Planar
 // pair windows hold a detector row as two FP32 rows, its values and then its
 // differences: four 4-byte loads per voxel, with the FP32 window's bank
-// pattern, but still one FFMA per row.  Separate from bp_tma.cu so that the
+// pattern, but still one FFMA per row.  FP16 pair windows (mixed precision)
+// hold each pair in 32 bits: one 4-byte load per row, the FP32 window's bytes
+// halved and its bank pattern kept.  Separate from bp_tma.cu so that the
 // two sets of instantiations compile in parallel.
 #include "bp_brick.cuh"
 
@@ -20,9 +22,17 @@ cudaError_t launch_backproject_tma_pairs(const CUtensorMap& map, const BpPlan& p
                                          cudaStream_t st) {
   if (plan.planar) {  // (planned for y-maps without a Z term only)
     if (!plan.bz0) return cudaErrorInvalidValue;
-    if (plan.lanes == 2) return launch_nz<float, 1, true, 2, true, true>(map, P, plan, st);
-    if (plan.lanes == 1) return launch_nz<float, 1, true, 1, true, true>(map, P, plan, st);
-    return launch_nz<float, 1, true, 0, true, true>(map, P, plan, st);
+    if (plan.lanes == 2) return launch_nz<float, 1, true, 2, true, 1>(map, P, plan, st);
+    if (plan.lanes == 1) return launch_nz<float, 1, true, 1, true, 1>(map, P, plan, st);
+    return launch_nz<float, 1, true, 0, true, 1>(map, P, plan, st);
+  }
+  if (plan.half) {
+    if (plan.lanes == 2) return plan.bz0 ? launch_nz<float, 1, true, 2, true, 2>(map, P, plan, st)
+                                         : launch_nz<float, 1, true, 2, false, 2>(map, P, plan, st);
+    if (plan.lanes == 1) return plan.bz0 ? launch_nz<float, 1, true, 1, true, 2>(map, P, plan, st)
+                                         : launch_nz<float, 1, true, 1, false, 2>(map, P, plan, st);
+    return plan.bz0 ? launch_nz<float, 1, true, 0, true, 2>(map, P, plan, st)
+                    : launch_nz<float, 1, true, 0, false, 2>(map, P, plan, st);
   }
   if (plan.lanes == 2) return plan.bz0 ? launch_nz<float, 1, true, 2, true>(map, P, plan, st)
                                        : launch_nz<float, 1, true, 2, false>(map, P, plan, st);

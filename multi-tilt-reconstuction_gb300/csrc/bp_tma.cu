@@ -217,12 +217,13 @@ namespace {
 BpPlan plan_backproject_uncached(const std::vector<double>& xc, const std::vector<double>& yc, int A, int fmt,
                                  int nz, int lane) {
   BpPlan p;
-  // FP32 and planar windows start on a 4-pixel (16-byte) boundary;
-  // interleaved pair windows on an even pair column (16 bytes of pairs)
+  // FP32, planar and FP16 pair windows start on a 4-element (16-byte)
+  // boundary; interleaved FP32 pair windows on an even pair column (16 bytes)
   const bool pairs = fmt == 1;
   p.align = pairs ? 2 : 4;
   p.pairs = fmt != 0;
   p.planar = fmt == 2;
+  p.half = fmt == 3;
   p.nz = nz;
   const size_t es = pairs ? 8 : 4;          // bytes per window element
   const int planes = p.planar ? 2 : 1;      // window rows per detector row

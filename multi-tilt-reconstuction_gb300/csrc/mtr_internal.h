@@ -119,6 +119,7 @@ struct BpPlan {
   int nz = 8;          // brick depth (voxels per thread along Z): 4, 8 or 16
   bool pairs = false;  // windows of residual pairs (SIRT update) rather than FP32 projections (WBP)
   bool planar = false; // pairs as two FP32 planes per row (values, differences) instead of interleaved
+  bool half = false;   // pairs as FP16 (value, difference) in 32 bits (mixed precision)
   size_t smem = 0;     // dynamic shared memory per CTA
 };
 extern const int kBpDepths[4];  // candidate brick depths of the SIRT back-projection
@@ -131,7 +132,8 @@ double window_bank_cost(const std::vector<double>& xc, const std::vector<double>
 // 1 = lines along Y, 2 = 8x4 patches.
 // pairs: windows of residual pairs for the SIRT update (false: FP32 windows
 // of the projections for the WBP).
-// fmt: 0 FP32 windows, 1 interleaved residual pairs, 2 planar residual pairs.
+// fmt: 0 FP32 windows, 1 interleaved residual pairs, 2 planar residual pairs,
+// 3 FP16 residual pairs (mixed precision).
 BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>& yc, int A, int fmt, int nz,
                         int lane = -1);
 // Row pitch (pairs) of the residual pair array of a detector PX pixels wide:
@@ -139,12 +141,13 @@ BpPlan plan_backproject(const std::vector<double>& xc, const std::vector<double>
 // padded to a multiple of 4 pairs (32-byte rows).
 inline int pair_pitch(int px) { return (px + 1 + 3) / 4 * 4; }
 // Residual in pair form: r = b - s/c (c != 0, else b - s) per detector row
-// (`rows` rows of `pitch` elements), written as pitch2 pairs per row, either
-// interleaved (value, difference) or planar (the row's values, then its
-// differences); s reset to zero; norm2: FP64 sum of r^2 (or null).
+// (`rows` rows of `pitch` elements), written as pitch2 pairs per row:
+// form 0 interleaved FP32 (value, difference), 1 planar (the row's values,
+// then its differences), 2 FP16 (value, difference) in 32 bits; s reset to
+// zero; norm2: FP64 sum of r^2 (or null).
 template <typename BT>
 void launch_residual_pairs(long long rows, int pitch, int pitch2, const BT* b, float* s, const float* c, float* rp,
-                           bool planar, double* norm2, cudaStream_t st);
+                           int form, double* norm2, cudaStream_t st);
 template <typename PT>
 cudaError_t launch_backproject_tma(const CUtensorMap& map, const BpPlan& plan, const AxisDev& ax,
                                    const VolDev& vol, int mode, float step, float* vol_out, float* cbp,

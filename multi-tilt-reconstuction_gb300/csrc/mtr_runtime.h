@@ -302,9 +302,11 @@ struct AxisState {
 // Tensor map over an axis' residual in pair form: FP32 elements, rows of
 // 2 * pitch2 floats, boxes of 2 * WX floats (WX pairs) by WY rows; planar
 // pairs as 2 * PY rows of pitch2 floats (each detector row's values, then its
-// differences), boxes of WX floats by 2 * WY rows.
+// differences), boxes of WX floats by 2 * WY rows; FP16 pairs as 32-bit
+// elements, rows of pitch2, boxes of WX by WY.
 inline bool encode_pair_map(CUtensorMap* m, const AxisState& a, const BpPlan& p) {
   if (!p.pairs) return false;
+  if (p.half) return encode_tensor_map_3d(m, a.r.p, false, a.pitch2, a.pitch2, a.PY, a.A, p.WX, p.WY);
   if (p.planar) return encode_tensor_map_3d(m, a.r.p, false, a.pitch2, a.pitch2, 2 * a.PY, a.A, p.WX, 2 * p.WY);
   return encode_tensor_map_3d(m, a.r.p, false, 2 * a.pitch2, 2 * a.pitch2, a.PY, a.A, 2 * p.WX, p.WY);
 }

@@ -284,9 +284,10 @@ residual_kernel(long long n, long long n4, const BT* __restrict__ b, float* __re
 // chunk; r[c-1] of a lane's first column comes from the lane below (lane 0:
 // the last column of the previous chunk).  s is reset to zero.  Returns the
 // lane's sum of r^2.
-// PLANAR: the row's pairs are written as two planes of pitch2 floats, the
-// values and then the differences (out is the row's first float).
-template <typename BT, bool PLANAR>
+// FORM 1: the row's pairs are written as two planes of pitch2 floats, the
+// values and then the differences (out is the row's first float); FORM 2:
+// as FP16 pairs, one 32-bit word each (out is the row's first word).
+template <typename BT, int FORM>
 __device__ __forceinline__ float residual_pair_row(const BT* __restrict__ br, float* __restrict__ sr,
                                                    const float* __restrict__ cr, float* __restrict__ out, int pitch,
                                                    int pitch2, int lane) {
@@ -309,8 +310,15 @@ __device__ __forceinline__ float residual_pair_row(const BT* __restrict__ br, fl
     float prev = __shfl_up_sync(0xffffffffu, r4[3], 1);
     if (lane == 0) prev = carry;
     carry = __shfl_sync(0xffffffffu, r4[3], 31);
-    if (col < pitch2) {  // pitch2 is a multiple of 4: four pairs, 32 bytes
-      if constexpr (PLANAR) {
+    if (col < pitch2) {  // pitch2 is a multiple of 4: four pairs, 32 bytes (16 in FP16)
+      if constexpr (FORM == 2) {
+        __half2 h[4];
+        h[0] = __floats2half2_rn(prev, r4[0] - prev);
+        h[1] = __floats2half2_rn(r4[0], r4[1] - r4[0]);
+        h[2] = __floats2half2_rn(r4[1], r4[2] - r4[1]);
+        h[3] = __floats2half2_rn(r4[2], r4[3] - r4[2]);
+        *reinterpret_cast<uint4*>(out + col) = *reinterpret_cast<const uint4*>(h);
+      } else if constexpr (FORM == 1) {
         *reinterpret_cast<float4*>(out + col) = make_float4(prev, r4[0], r4[1], r4[2]);
         *reinterpret_cast<float4*>(out + pitch2 + col) =
             make_float4(r4[0] - prev, r4[1] - r4[0], r4[2] - r4[1], r4[3] - r4[2]);
@@ -325,7 +333,7 @@ __device__ __forceinline__ float residual_pair_row(const BT* __restrict__ br, fl
 }
 
 // One warp per detector row (rows = AngN * PY); FP64 norm when NORM.
-template <typename BT, bool NORM, bool PLANAR>
+template <typename BT, bool NORM, int FORM>
 __global__ void __launch_bounds__(256)
 residual_pairs_kernel(long long rows, int pitch, int pitch2, const BT* __restrict__ b, float* __restrict__ s,
                       const float* __restrict__ c, float* __restrict__ rp, double* __restrict__ norm2) {
@@ -333,8 +341,8 @@ residual_pairs_kernel(long long rows, int pitch, int pitch2, const BT* __restric
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   double acc = 0.0;
   for (long long row = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; row < rows; row += nwarps) {
-    const float sq = residual_pair_row<BT, PLANAR>(b + row * pitch, s + row * pitch, c + row * pitch,
-                                                   rp + row * 2 * pitch2, pitch, pitch2, lane);
+    const float sq = residual_pair_row<BT, FORM>(b + row * pitch, s + row * pitch, c + row * pitch,
+                                                 rp + row * (FORM == 2 ? 1 : 2) * pitch2, pitch, pitch2, lane);
     if (NORM) acc += (double)sq;
   }
   if (NORM) {
@@ -417,24 +425,27 @@ void launch_residual_batch(const ResBatchDesc* descs, const long long* first, in
 
 template <typename BT>
 void launch_residual_pairs(long long rows, int pitch, int pitch2, const BT* b, float* s, const float* c, float* rp,
-                           bool planar, double* norm2, cudaStream_t st) {
+                           int form, double* norm2, cudaStream_t st) {
   long long blocks = (rows + 7) / 8;  // 8 warps per block, one row per warp
   const long long cap = (long long)device_sm_count() * 16;
   if (blocks > cap) blocks = cap;  // grid-stride over the rest
   if (blocks < 1) blocks = 1;
   const unsigned g = (unsigned)blocks;
-  if (planar) {
-    if (norm2) residual_pairs_kernel<BT, true, true><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
-    else residual_pairs_kernel<BT, false, true><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
+  if (form == 2) {
+    if (norm2) residual_pairs_kernel<BT, true, 2><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
+    else residual_pairs_kernel<BT, false, 2><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
+  } else if (form == 1) {
+    if (norm2) residual_pairs_kernel<BT, true, 1><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
+    else residual_pairs_kernel<BT, false, 1><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
   } else {
-    if (norm2) residual_pairs_kernel<BT, true, false><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
-    else residual_pairs_kernel<BT, false, false><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
+    if (norm2) residual_pairs_kernel<BT, true, 0><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, norm2);
+    else residual_pairs_kernel<BT, false, 0><<<g, 256, 0, st>>>(rows, pitch, pitch2, b, s, c, rp, nullptr);
   }
 }
 
-template void launch_residual_pairs<float>(long long, int, int, const float*, float*, const float*, float*, bool,
+template void launch_residual_pairs<float>(long long, int, int, const float*, float*, const float*, float*, int,
                                            double*, cudaStream_t);
-template void launch_residual_pairs<__half>(long long, int, int, const __half*, float*, const float*, float*, bool,
+template void launch_residual_pairs<__half>(long long, int, int, const __half*, float*, const float*, float*, int,
                                             double*, cudaStream_t);
 
 template void launch_backproject<float>(const AxisDev&, const VolDev&, const float*, int, float, float*, float*,

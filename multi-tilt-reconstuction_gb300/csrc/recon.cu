@@ -195,10 +195,10 @@ mtr_status enqueue_residual(mtr_recon* r, AxisState& a, double* norm) {
   if (a.tma && a.plan.pairs) {  // this axis' windowed update reads (value, next - value) pairs
     if (mixed(r->p.precision))
       launch_residual_pairs<__half>(rows, a.pitch, a.pitch2, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(),
-                                    a.r.as<float>(), a.plan.planar, norm, ctx->stream);
+                                    a.r.as<float>(), a.plan.half ? 2 : a.plan.planar ? 1 : 0, norm, ctx->stream);
     else
       launch_residual_pairs<float>(rows, a.pitch, a.pitch2, a.b.as<float>(), a.s.as<float>(), a.cf.as<float>(),
-                                   a.r.as<float>(), a.plan.planar, norm, ctx->stream);
+                                   a.r.as<float>(), a.plan.planar ? 1 : 0, norm, ctx->stream);
   } else if (mixed(r->p.precision)) {
     launch_residual<__half, float>(a.np, a.b.as<__half>(), a.s.as<float>(), a.cf.as<float>(), a.r.as<float>(), norm,
                                    ctx->stream);
@@ -853,7 +853,8 @@ mtr_status mtr_recon_describe(const mtr_recon* r, char* buf, int cap) {
                   "\"window_format\":\"%s\"},"
                   "\"forward\":{\"tma\":%s,\"depth\":%d,\"window\":[%d,%d],\"lanes\":\"%s\",\"y_has_z\":%s}}",
                   k ? "," : "", k, a.tma ? "true" : "false", a.plan.nz, a.plan.WX, a.plan.WY,
-                  a.plan.lanes == 1 ? "y" : a.plan.lanes == 2 ? "patch" : "x", a.plan.planar ? "planar pairs" : a.plan.pairs ? "pairs" : "fp32",
+                  a.plan.lanes == 1 ? "y" : a.plan.lanes == 2 ? "patch" : "x",
+                  a.plan.half ? "fp16 pairs" : a.plan.planar ? "planar pairs" : a.plan.pairs ? "pairs" : "fp32",
                   a.ftma ? "true" : "false", a.fplan.nz, a.fplan.WX, a.fplan.WY,
                   a.fplan.lanes == 1 ? "y" : a.fplan.lanes == 2 ? "patch" : "x", a.fplan.bz0 ? "false" : "true");
     s += t;

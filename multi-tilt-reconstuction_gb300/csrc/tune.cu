@@ -15,7 +15,8 @@
 //    window and load 8 bytes per lane (faster where a warp's lanes share
 //    detector rows, slower where their 8-byte loads conflict in the banks),
 //    or the same pairs as two FP32 planes per row (4-byte loads with the FP32
-//    window's bank pattern, one FFMA per row).
+//    window's bank pattern, one FFMA per row), or (mixed precision) FP16
+//    pairs in 32 bits (one 4-byte load per row: half the shared-memory bytes).
 // For each tilt axis the tuner times every candidate (3 formats x depth
 // 4/8/16/32 x lines along X / lines along Y / patches for the SIRT
 // back-projection, depth 8/16/32 x the same three layouts for the forward
@@ -25,9 +26,10 @@
 // keeps the fastest.  Results are cached per process by a geometry key and,
 // when MTR_AUTOTUNE_CACHE names a file, persisted there as JSON ({"key":
 // [bp_depth, fwd_depth, bp_lane, fwd_lane, bp_format], ...}; bp_format 0 FP32
-// windows, 1 interleaved pairs, 2 planar pairs).  MTR_AUTOTUNE=0 disables
+// windows, 1 interleaved pairs, 2 planar pairs, 3 FP16 pairs in mixed precision).  MTR_AUTOTUNE=0 disables
 // tuning (depths 8 and 16, lane axis by slope, FP32 windows);
-// MTR_FORCE_DEPTHS=bp,fwd[,bp_lane,fwd_lane[,bp_format]] pins the choice.
+// MTR_FORCE_DEPTHS=bp,fwd[,bp_lane,fwd_lane[,bp_format]] pins the choice;
+// MTR_AUTOTUNE_LOG=1 prints every candidate's time to stderr.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -119,7 +121,8 @@ std::string geometry_key(const AxisState& a, const VolDev& v, int precision) {
 // are timed round-robin for kRounds rounds and each keeps its minimum, so a
 // clock ramp during tuning does not favour the candidates timed last.
 constexpr int kRounds = 3;
-int fastest(cudaStream_t st, const std::vector<std::function<cudaError_t()>>& cands) {
+int fastest(cudaStream_t st, const std::vector<std::function<cudaError_t()>>& cands, const char* log_to = nullptr,
+            const std::vector<std::string>* what = nullptr) {
   const size_t n = cands.size();
   std::vector<float> best(n, 1e30f);
   std::vector<bool> ok(n, false);
@@ -150,7 +153,18 @@ int fastest(cudaStream_t st, const std::vector<std::function<cudaError_t()>>& ca
   int arg = -1;
   for (size_t i = 0; i < n; ++i)
     if (ok[i] && (arg < 0 || best[i] < best[arg])) arg = (int)i;
+  if (log_to) {
+    for (size_t i = 0; i < n; ++i)
+      std::fprintf(stderr, "mtr autotune %s %s %s: %.4f ms%s\n", log_to, what ? (*what)[i].c_str() : "", ok[i] ? "" : "failed",
+                   ok[i] ? best[i] : 0.f, (int)i == arg ? "  <- chosen" : "");
+  }
   return arg;
+}
+
+// MTR_AUTOTUNE_LOG=1 prints every candidate's best time to stderr.
+bool autotune_log() {
+  const char* e = std::getenv("MTR_AUTOTUNE_LOG");
+  return e && e[0] == '1';
 }
 
 }  // namespace
@@ -209,9 +223,11 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
     std::vector<BpPlan> bps;
     std::vector<CUtensorMap> bmaps;
     // (the candidates keep pointers into these: no reallocation)
-    bps.reserve(9 * std::size(kBpDepths));  // 3 formats x 3 lane layouts x the depths
-    bmaps.reserve(9 * std::size(kBpDepths));
-    for (int fmt = 0; fmt < 3; ++fmt)
+    // (FP16 residual pairs only in mixed precision)
+    const int n_fmt = copy_kind != 0 ? 4 : 3;
+    bps.reserve(12 * std::size(kBpDepths));  // formats x 3 lane layouts x the depths
+    bmaps.reserve(12 * std::size(kBpDepths));
+    for (int fmt = 0; fmt < n_fmt; ++fmt)
       for (int lane = 0; lane < 3; ++lane)
         for (int nz : kBpDepths) {
           BpPlan p = plan_backproject(a.hxc, a.hyc, a.A, fmt, nz, lane);
@@ -231,7 +247,14 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
           c.bp_pairs = fmt;
           what.push_back(c);
         }
-    int k = fastest(ctx->stream, cands);
+    const bool log = autotune_log();
+    std::vector<std::string> labels;
+    char lb[96];
+    for (const Choice& c : what) {
+      std::snprintf(lb, sizeof(lb), "bp fmt %d lane %d depth %d", c.bp_pairs, c.bp_lane, c.bp_nz);
+      labels.push_back(lb);
+    }
+    int k = fastest(ctx->stream, cands, log ? key.c_str() : nullptr, &labels);
     if (k >= 0) {
       ch.bp_nz = what[k].bp_nz;
       ch.bp_lane = what[k].bp_lane;
@@ -269,7 +292,12 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
         c.fwd_lane = lane;
         what.push_back(c);
       }
-    k = fastest(ctx->stream, cands);
+    labels.clear();
+    for (const Choice& c : what) {
+      std::snprintf(lb, sizeof(lb), "fwd lane %d depth %d", c.fwd_lane, c.fwd_nz);
+      labels.push_back(lb);
+    }
+    k = fastest(ctx->stream, cands, log ? key.c_str() : nullptr, &labels);
     if (k >= 0) {
       ch.fwd_nz = what[k].fwd_nz;
       ch.fwd_lane = what[k].fwd_lane;
@@ -280,7 +308,8 @@ bool tune_axis(mtr_context* ctx, AxisState& a, const VolDev& v, int precision, f
   }
   // the timing runs wrote into s and the tuner's scratch: restore the zeros
   cudaMemsetAsync(a.s.p, 0, (size_t)a.np * 4, ctx->stream);
-  a.plan = plan_backproject(a.hxc, a.hyc, a.A, std::min(std::max(ch.bp_pairs, 0), 2), ch.bp_nz, ch.bp_lane);
+  a.plan = plan_backproject(a.hxc, a.hyc, a.A, std::min(std::max(ch.bp_pairs, 0), copy_kind != 0 ? 3 : 2), ch.bp_nz,
+                            ch.bp_lane);
   a.tma = a.plan.ok && encode_residual_map(&a.map_r, a, a.plan);
   a.fplan = plan_forward(a.hxc, a.hyc, a.A, a.PX, a.PY, a.pitch, ch.fwd_nz, ch.fwd_lane);
   a.ftma = a.fplan.ok &&

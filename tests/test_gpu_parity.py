@@ -206,6 +206,37 @@ def test_every_brick_depth_matches_oracle(ctx, monkeypatch, name, depths):
     assert rel_l2(got, want) < FP32_TOL
 
 
+# ... over FP16 residual-pair windows (mixed precision only; FP32 runs clamp
+# the format to planar FP32 pairs)
+@pytest.mark.parametrize("depths", ["16,32,2,0,3", "8,16,0,1,3", "32,8,1,2,3", "4,32,2,2,3", "32,32,0,0,3"])
+@pytest.mark.parametrize("name", ["mid", "mid_oblique"])
+def test_fp16_pair_windows_match_fp64_oracle(ctx, monkeypatch, name, depths):
+    monkeypatch.setenv("MTR_FORCE_DEPTHS", depths)
+    c = cases.get(name)
+    p = mtr.params(iter_times=1, sirt_inner=3, sirt_step=0.5, mace_step=0.7, precision=mtr.PREC_MIXED_FP16)
+    r = mtr.Recon(ctx, c.axes, c.vol, p)
+    try:
+        assert all(d["back_projection"]["window_format"] == "fp16 pairs" for d in r.describe())
+        r.run()
+        got = r.download()
+    finally:
+        r.close()
+    want = oracle.reconstruct(oracle.FP64, c.axes, c.vol, 1, 3, 0.5, 0.7)
+    assert rel_l2(got, want) < MIXED_TOL
+    p32 = mtr.params(iter_times=1, sirt_inner=3, sirt_step=0.5, mace_step=0.7)
+    got32 = ctx.reconstruct(c.axes, c.vol, p32)
+    assert rel_l2(got32, oracle.reconstruct(oracle.REF_FAITHFUL, c.axes, c.vol, 1, 3, 0.5, 0.7)) < FP32_TOL
+
+
+def test_fp16_pair_windows_z_dependent_y_map(ctx, monkeypatch):
+    monkeypatch.setenv("MTR_FORCE_DEPTHS", "8,16,0,0,3")
+    c = cases.tilt_axis_in_z(cases.get("mid"))
+    p = mtr.params(iter_times=1, sirt_inner=4, sirt_step=0.5, mace_step=0.7, precision=mtr.PREC_MIXED_FP16)
+    got = ctx.reconstruct(c.axes, c.vol, p)
+    want = oracle.reconstruct(oracle.FP64, c.axes, c.vol, 1, 4, 0.5, 0.7)
+    assert rel_l2(got, want) < MIXED_TOL
+
+
 def test_autotune_cache_file(ctx, monkeypatch, tmp_path):
     import json
 
@@ -219,7 +250,7 @@ def test_autotune_cache_file(ctx, monkeypatch, tmp_path):
     d = json.loads(cache.read_text())
     # lane -1: no windowed candidate fits that detector (the plain kernel runs)
     assert d and all(b in (4, 8, 16, 32) and f in (8, 16, 32) and bl in (-1, 0, 1, 2) and fl in (-1, 0, 1, 2)
-                     and bp in (0, 1, 2) for b, f, bl, fl, bp in d.values())
+                     and bp in (0, 1, 2, 3) for b, f, bl, fl, bp in d.values())
     key = next(k for k in d if k.startswith("p72x72x13_v64x48x19"))
     assert d[key][2] in (0, 1, 2) and d[key][3] in (0, 1, 2)  # this detector fits both windowed kernels
 
