@@ -90,75 +90,105 @@ template <> __device__ __forceinline__ float ldv<__half>(const void* p, long lon
   return __half2float(__ldg(static_cast<const __half*>(p) + i));
 }
 
-// Streaming splat of one voxel column (fixed X, Y; y-map without a Z term)
-// into detector rows `row` and `row + WX`.  x advances by |a3| < 1 per voxel,
-// so consecutive voxels reach at most one new pixel: the column's 1-D splat is
-// accumulated in registers and a pixel is emitted (one integer add per row,
-// its y weights wy0 / wy1 factored out of the column) only when the column
-// moves past it.  ASC walks z upwards (a3 >= 0), else downwards, so that x
-// never decreases.
-template <bool ASC, int NZ>
+// Streaming splat of one voxel column (fixed X, Y; y-map without a Z term):
+// its detector y (rows and weights wy0 / wy1) is common to the column and
+// its detector x moves by |a3| < 1 per voxel, so consecutive voxels reach at
+// most one new pixel.  The column's 1-D splat is accumulated in registers and
+// a pixel is emitted (one integer add per detector row) only once the column
+// has left it.  ROW: the warp's lanes share their rows and weights, so the
+// unsplit values go into the warp's row buffer `row` (one add per pixel; the
+// warp splits the row afterwards), else into detector rows `row` and
+// `row + WX`.
+//
+// The walk always runs z upwards.  Where a3 < 0 it runs in the mirrored
+// coordinate u = -x, which grows by |a3| per voxel: a voxel at u with
+// fraction f splats (1 - f, f) onto mirrored pixels (p, p + 1), which are the
+// original pixels (-p, -p - 1) with the original splat's weights, so the
+// emissions go to window column (xi - ox) - p.  One code path serves both
+// slope signs (half the unrolled code of a walk per sign).
+//
+// L > 1 (slope below 1 / L): a chunk of L voxels crosses at most one pixel
+// boundary, so it accumulates without a branch and the column emits at most
+// once per chunk; branching per voxel made the warp run the emission on
+// almost every voxel (its lanes cross at different voxels).  S is the weight
+// not yet emitted (pixels p and p + 1), a1 its part on p + 1.  Inside a chunk
+// the fraction runs on past 1: a voxel beyond the crossing (fraction f in
+// [1, 2)) is first added as if it were not (1 - f on p, f on p + 1) and C
+// collects (f - 1) v, which moves it to its true pixels (2 - f on p + 1,
+// f - 1 on p + 2) when the chunk ends.
+template <int NZ, int L, bool ROW>
 __device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)[NZ], float xr, float a3, int lxm,
                                               float wy0, float wy1) {
-  constexpr int zf = ASC ? 0 : NZ - 1;
-  const float x = fmaf(a3, (float)zf, xr);
-  const float flx = floorf(x);
-  float fx = x - flx;
+  const int dir = a3 >= 0.f ? 1 : -1;
+  const float u = a3 >= 0.f ? xr : -xr;
+  const float flu = floorf(u);
+  float fx = u - flu;
   const float step = fabsf(a3);
-  int cur = magic_int(flx) + lxm;
-  float acc0 = (1.f - fx) * v[zf], acc1 = fx * v[zf];
-#pragma unroll
-  for (int i = 1; i < NZ; ++i) {
-    const int z = ASC ? i : NZ - 1 - i;
-    // the fraction is stepped (rounding < 4e-6 px over 32 voxels; the window
-    // keeps one pixel of slack past the last exact tap for it)
-    fx += step;
-    if (fx >= 1.f) {  // the column left pixel `cur`
-      fx -= 1.f;
-      atomicAdd(row + cur, fixq(wy0, acc0));
-      atomicAdd(row + WX + cur, fixq(wy1, acc0));
-      acc0 = acc1;
-      acc1 = 0.f;
-      ++cur;
+  // window column of pixel p: (xi - ox) + dir * p, with xi - ox = lxm + kMagicBits
+  int* at = row + ((lxm + kMagicBits) + dir * (magic_int(flu) - kMagicBits));
+  auto emit = [&](int* q, float e) {
+    if (ROW) {
+      atomicAdd(q, fixq(1.f, e));
+    } else {
+      atomicAdd(q, fixq(wy0, e));
+      atomicAdd(q + WX, fixq(wy1, e));
     }
-    acc0 = fmaf(1.f - fx, v[z], acc0);
-    acc1 = fmaf(fx, v[z], acc1);
+  };
+  if constexpr (L == 1) {
+    float acc0 = (1.f - fx) * v[0], acc1 = fx * v[0];
+#pragma unroll
+    for (int z = 1; z < NZ; ++z) {
+      // the fraction is stepped (rounding < 4e-6 px over 32 voxels; the window
+      // keeps one pixel of slack past the last exact tap on either side)
+      fx += step;
+      if (fx >= 1.f) {  // the column left the pixel at `at`
+        fx -= 1.f;
+        emit(at, acc0);
+        acc0 = acc1;
+        acc1 = 0.f;
+        at += dir;
+      }
+      acc0 = fmaf(1.f - fx, v[z], acc0);
+      acc1 = fmaf(fx, v[z], acc1);
+    }
+    emit(at, acc0);
+    emit(at + dir, acc1);
+  } else {
+    float S = v[0], a1 = fx * v[0];
+#pragma unroll
+    for (int z0 = 1; z0 < NZ; z0 += L) {
+      float C = 0.f;
+#pragma unroll
+      for (int j = 0; j < L; ++j) {
+        if (z0 + j < NZ) {
+          fx += step;
+          S += v[z0 + j];
+          a1 = fmaf(fx, v[z0 + j], a1);
+          C = fmaf(__saturatef(fx - 1.f), v[z0 + j], C);  // f - 1 < 1: saturation is max(f - 1, 0)
+        }
+      }
+      if (fx >= 1.f) {  // the chunk left the pixel at `at`
+        emit(at, (S - a1) + C);
+        S = a1 - C;
+        a1 = C;
+        fx -= 1.f;
+        at += dir;
+      }
+    }
+    emit(at, S - a1);
+    emit(at + dir, a1);
   }
-  atomicAdd(row + cur, fixq(wy0, acc0));
-  atomicAdd(row + WX + cur, fixq(wy1, acc0));
-  atomicAdd(row + cur + 1, fixq(wy0, acc1));
-  atomicAdd(row + WX + cur + 1, fixq(wy1, acc1));
 }
 
-// stream_column for a warp whose lanes all splat into the same two detector
-// rows with the same y weights: the column emits its unsplit fixed-point
-// values into the warp's own row buffer `u` (one atomic per pixel instead of
-// two); the warp splits that row into the two detector rows afterwards.
-template <bool ASC, int NZ>
-__device__ __forceinline__ void stream_column_row(int* u, const float (&v)[NZ], float xr, float a3, int lxm) {
-  constexpr int zf = ASC ? 0 : NZ - 1;
-  const float x = fmaf(a3, (float)zf, xr);
-  const float flx = floorf(x);
-  float fx = x - flx;
-  const float step = fabsf(a3);
-  int cur = magic_int(flx) + lxm;
-  float acc0 = (1.f - fx) * v[zf], acc1 = fx * v[zf];
-#pragma unroll
-  for (int i = 1; i < NZ; ++i) {
-    const int z = ASC ? i : NZ - 1 - i;
-    fx += step;
-    if (fx >= 1.f) {
-      fx -= 1.f;
-      atomicAdd(u + cur, fixq(1.f, acc0));
-      acc0 = acc1;
-      acc1 = 0.f;
-      ++cur;
-    }
-    acc0 = fmaf(1.f - fx, v[z], acc0);
-    acc1 = fmaf(fx, v[z], acc1);
-  }
-  atomicAdd(u + cur, fixq(1.f, acc0));
-  atomicAdd(u + cur + 1, fixq(1.f, acc1));
+// stream_column with the longest chunk the slope allows (the bounds leave
+// room for the stepped fraction's rounding: a chunk's fraction stays below 2).
+template <int NZ, bool ROW>
+__device__ __forceinline__ void splat_column(int* row, int WX, const float (&v)[NZ], float xr, float a3, int lxm,
+                                             float wy0, float wy1) {
+  const float st = fabsf(a3);
+  if (st < 0.2499f) stream_column<NZ, 4, ROW>(row, WX, v, xr, a3, lxm, wy0, wy1);
+  else if (st < 0.4999f) stream_column<NZ, 2, ROW>(row, WX, v, xr, a3, lxm, wy0, wy1);
+  else stream_column<NZ, 1, ROW>(row, WX, v, xr, a3, lxm, wy0, wy1);
 }
 
 // One brick (bx, by, zb) and angle group g of one axis; `smem` is the CTA's
@@ -271,10 +301,7 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
     if (BZ0 && LANES != 2 && k.interior && fabsf(k.a3) < 0.999f && fabsf(LANES == 1 ? k.b2 : k.b1) < 3e-8f) {
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
       const float yr = __shfl_sync(0xffffffffu, fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf)), 0);
-      if (active) {
-        if (k.a3 >= 0.f) stream_column_row<true, NZ>(urow, v, xr, k.a3, k.lxm);
-        else stream_column_row<false, NZ>(urow, v, xr, k.a3, k.lxm);
-      }
+      if (active) splat_column<NZ, true>(urow, WX, v, xr, k.a3, k.lxm, 1.f, 0.f);
       __syncwarp();
       // split the warp's row into the two detector rows (values up to 2^30:
       // rounded with a conversion, the magic-number rounding needs < 2^22)
@@ -297,8 +324,7 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
       const float fly = floorf(yr);
       const float fy = yr - fly;
       int* rowp = wi + (magic_int(fly) + k.lym) * WX;
-      if (k.a3 >= 0.f) stream_column<true, NZ>(rowp, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy);
-      else stream_column<false, NZ>(rowp, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy);
+      splat_column<NZ, false>(rowp, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy);
     } else if (active && BZ0 && k.interior) {
       // every tap lands in the window and on the detector: no per-tap tests
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
