@@ -532,8 +532,9 @@ __device__ __forceinline__ void bp_brick(const CUtensorMap* tmap, const BpArgs& 
 // bricks of the same rows at all depths run together, so the detector rows
 // they read stay in L2 instead of being re-read from DRAM once per z layer.
 template <typename PT, int MODE, bool PAIR, int LANES, bool BZ0, int NZ, int PF = 0>
-// (FP32 pair windows take twice the shared memory: 4 CTAs per SM below depth 32)
-__global__ void __launch_bounds__(kThreads, MODE == 1 ? (NZ >= 32 ? 3 : (PAIR && PF != 2 ? 4 : 5)) : 4)
+// (FP32 pair windows take twice the shared memory: 4 CTAs per SM below depth 32;
+// at depth 32 the 32 accumulators fit the 56 registers of 4 CTAs per SM)
+__global__ void __launch_bounds__(kThreads, MODE == 1 ? (NZ >= 32 ? 4 : (PAIR && PF != 2 ? 4 : 5)) : 4)
 bp_tma_kernel(const __grid_constant__ CUtensorMap tmap, const BpArgs P) {
   extern __shared__ __align__(128) unsigned char smem[];
   bp_brick<PT, MODE, PAIR, LANES, BZ0, NZ, PF>(&tmap, P, blockIdx.x, blockIdx.z, blockIdx.y, smem, false);
