@@ -78,6 +78,11 @@ __device__ __forceinline__ void zero_window(int* w, int n) {
 __device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b : -((-a + b - 1) / b); }
 // round(w * v) for |w*v| < 2^22, as an integer, without a conversion instruction
 __device__ __forceinline__ int fixq(float w, float v) { return __float_as_int(fmaf(w, v, kMagic)) - kMagicBits; }
+// Integer add to the shared-memory word at 32-bit shared address `addr`
+// (no value returned; the column walks keep their addresses in this form).
+__device__ __forceinline__ void red_shared(uint32_t addr, int v) {
+  asm volatile("red.shared.add.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
 
 template <typename VT> __device__ __forceinline__ float ldv(const void* p, long long i);
 template <> __device__ __forceinline__ float ldv<float>(const void* p, long long i) {
@@ -124,14 +129,16 @@ __device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)
   const float flu = floorf(u);
   float fx = u - flu;
   const float step = fabsf(a3);
-  // window column of pixel p: (xi - ox) + dir * p, with xi - ox = lxm + kMagicBits
-  int* at = row + ((lxm + kMagicBits) + dir * (magic_int(flu) - kMagicBits));
-  auto emit = [&](int* q, float e) {
+  // window column of pixel p: (xi - ox) + dir * p, with xi - ox = lxm + kMagicBits;
+  // `at` is the shared address of the current pixel, `dstep` the next pixel's offset
+  uint32_t at = smem_u32(row) + 4u * (uint32_t)((lxm + kMagicBits) + dir * (magic_int(flu) - kMagicBits));
+  const uint32_t dstep = dir > 0 ? 4u : 0xFFFFFFFCu, drow = 4u * (uint32_t)WX;
+  auto emit = [&](uint32_t q, float e) {
     if (ROW) {
-      atomicAdd(q, fixq(1.f, e));
+      red_shared(q, fixq(1.f, e));
     } else {
-      atomicAdd(q, fixq(wy0, e));
-      atomicAdd(q + WX, fixq(wy1, e));
+      red_shared(q, fixq(wy0, e));
+      red_shared(q + drow, fixq(wy1, e));
     }
   };
   if constexpr (L == 1) {
@@ -146,13 +153,13 @@ __device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)
         emit(at, acc0);
         acc0 = acc1;
         acc1 = 0.f;
-        at += dir;
+        at += dstep;
       }
       acc0 = fmaf(1.f - fx, v[z], acc0);
       acc1 = fmaf(fx, v[z], acc1);
     }
     emit(at, acc0);
-    emit(at + dir, acc1);
+    emit(at + dstep, acc1);
   } else {
     float S = v[0], a1 = fx * v[0];
 #pragma unroll
@@ -172,11 +179,11 @@ __device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)
         S = a1 - C;
         a1 = C;
         fx -= 1.f;
-        at += dir;
+        at += dstep;
       }
     }
     emit(at, S - a1);
-    emit(at + dir, a1);
+    emit(at + dstep, a1);
   }
 }
 
