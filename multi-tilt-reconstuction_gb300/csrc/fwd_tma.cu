@@ -121,9 +121,15 @@ template <> __device__ __forceinline__ float ldv<__half>(const void* p, long lon
 // [1, 2)) is first added as if it were not (1 - f on p, f on p + 1) and C
 // collects (f - 1) v, which moves it to its true pixels (2 - f on p + 1,
 // f - 1 on p + 2) when the chunk ends.
-template <int NZ, int L, bool ROW>
-__device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)[NZ], float xr, float a3, int lxm,
-                                              float wy0, float wy1) {
+//
+// CHK: the brick's window is clamped at the detector edge (or reaches past
+// it), so some of the column's pixels are off the detector: each emission
+// checks its window column against the valid columns (span = 4 * valid
+// columns, in bytes) and each detector row against the window (y0ok, y1ok),
+// and drops what falls outside, as the reference drops off-detector taps.
+template <int NZ, int L, bool ROW, bool CHK>
+__device__ __forceinline__ void stream_column(uint32_t row, int WX, const float (&v)[NZ], float xr, float a3, int lxm,
+                                              float wy0, float wy1, uint32_t span, bool y0ok, bool y1ok) {
   const int dir = a3 >= 0.f ? 1 : -1;
   const float u = a3 >= 0.f ? xr : -xr;
   const float flu = floorf(u);
@@ -131,11 +137,15 @@ __device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)
   const float step = fabsf(a3);
   // window column of pixel p: (xi - ox) + dir * p, with xi - ox = lxm + kMagicBits;
   // `at` is the shared address of the current pixel, `dstep` the next pixel's offset
-  uint32_t at = smem_u32(row) + 4u * (uint32_t)((lxm + kMagicBits) + dir * (magic_int(flu) - kMagicBits));
+  uint32_t at = row + 4u * (uint32_t)((lxm + kMagicBits) + dir * (magic_int(flu) - kMagicBits));
   const uint32_t dstep = dir > 0 ? 4u : 0xFFFFFFFCu, drow = 4u * (uint32_t)WX;
   auto emit = [&](uint32_t q, float e) {
     if (ROW) {
       red_shared(q, fixq(1.f, e));
+    } else if (CHK) {
+      const bool xok = q - row < span;  // (a column left of the window wraps to a large offset)
+      if (xok && y0ok) red_shared(q, fixq(wy0, e));
+      if (xok && y1ok) red_shared(q + drow, fixq(wy1, e));
     } else {
       red_shared(q, fixq(wy0, e));
       red_shared(q + drow, fixq(wy1, e));
@@ -189,13 +199,14 @@ __device__ __forceinline__ void stream_column(int* row, int WX, const float (&v)
 
 // stream_column with the longest chunk the slope allows (the bounds leave
 // room for the stepped fraction's rounding: a chunk's fraction stays below 2).
-template <int NZ, bool ROW>
-__device__ __forceinline__ void splat_column(int* row, int WX, const float (&v)[NZ], float xr, float a3, int lxm,
-                                             float wy0, float wy1) {
+template <int NZ, bool ROW, bool CHK>
+__device__ __forceinline__ void splat_column(uint32_t row, int WX, const float (&v)[NZ], float xr, float a3, int lxm,
+                                             float wy0, float wy1, uint32_t span = 0, bool y0ok = true,
+                                             bool y1ok = true) {
   const float st = fabsf(a3);
-  if (st < 0.2499f) stream_column<NZ, 4, ROW>(row, WX, v, xr, a3, lxm, wy0, wy1);
-  else if (st < 0.4999f) stream_column<NZ, 2, ROW>(row, WX, v, xr, a3, lxm, wy0, wy1);
-  else stream_column<NZ, 1, ROW>(row, WX, v, xr, a3, lxm, wy0, wy1);
+  if (st < 0.2499f) stream_column<NZ, 4, ROW, CHK>(row, WX, v, xr, a3, lxm, wy0, wy1, span, y0ok, y1ok);
+  else if (st < 0.4999f) stream_column<NZ, 2, ROW, CHK>(row, WX, v, xr, a3, lxm, wy0, wy1, span, y0ok, y1ok);
+  else stream_column<NZ, 1, ROW, CHK>(row, WX, v, xr, a3, lxm, wy0, wy1, span, y0ok, y1ok);
 }
 
 // One brick (bx, by, zb) and angle group g of one axis; `smem` is the CTA's
@@ -308,7 +319,7 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
     if (BZ0 && LANES != 2 && k.interior && fabsf(k.a3) < 0.999f && fabsf(LANES == 1 ? k.b2 : k.b1) < 3e-8f) {
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
       const float yr = __shfl_sync(0xffffffffu, fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf)), 0);
-      if (active) splat_column<NZ, true>(urow, WX, v, xr, k.a3, k.lxm, 1.f, 0.f);
+      if (active) splat_column<NZ, true, false>(smem_u32(urow), WX, v, xr, k.a3, k.lxm, 1.f, 0.f);
       __syncwarp();
       // split the warp's row into the two detector rows (values up to 2^30:
       // rounded with a conversion, the magic-number rounding needs < 2^22)
@@ -324,14 +335,20 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
           urow[i] = 0;
         }
       }
-    } else if (active && BZ0 && k.interior && fabsf(k.a3) < 0.999f) {
-      // every tap lands in the window and on the detector; stream the column
+    } else if (active && BZ0 && fabsf(k.a3) < 0.999f) {
+      // stream the column; at an interior window every tap lands in the
+      // window and on the detector, elsewhere each emission is checked
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
       const float yr = fmaf(k.b2, (float)ty, fmaf(k.b1, (float)tx, k.yf));
       const float fly = floorf(yr);
       const float fy = yr - fly;
-      int* rowp = wi + (magic_int(fly) + k.lym) * WX;
-      splat_column<NZ, false>(rowp, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy);
+      const int rowi = magic_int(fly) + k.lym;
+      const uint32_t rowa = smem_u32(wi) + 4u * (uint32_t)(rowi * WX);
+      if (k.interior)
+        splat_column<NZ, false, false>(rowa, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy);
+      else
+        splat_column<NZ, false, true>(rowa, WX, v, xr, k.a3, k.lxm, 1.f - fy, fy, 4u * (uint32_t)k.wlx,
+                                      (unsigned)rowi < (unsigned)WY, (unsigned)(rowi + 1) < (unsigned)WY);
     } else if (active && BZ0 && k.interior) {
       // every tap lands in the window and on the detector: no per-tap tests
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
