@@ -61,10 +61,30 @@ __device__ __forceinline__ int floor_div(int a, int b) { return (a >= 0) ? a / b
 
 __device__ __forceinline__ int magic_int(float integral) { return __float_as_int(__fadd_rn(integral, kMagic)); }
 
+// Shared-memory loads at a 32-bit shared address plus a constant byte offset:
+// the column gathers step their tap address in this form (one 32-bit add per
+// pixel crossed) instead of a generic pointer.  Volatile keeps them after the
+// pipeline's mbarrier waits.
+template <int OFF> __device__ __forceinline__ float lds_f32(uint32_t a) {
+  float v;
+  asm volatile("ld.shared.f32 %0, [%1+%2];" : "=f"(v) : "r"(a), "n"(OFF));
+  return v;
+}
+template <int OFF> __device__ __forceinline__ float2 lds_f32x2(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2+%3];" : "=f"(v.x), "=f"(v.y) : "r"(a), "n"(OFF));
+  return v;
+}
+template <int OFF> __device__ __forceinline__ float2 lds_h2_widened(uint32_t a) {
+  __half2 h;
+  asm volatile("ld.shared.b32 %0, [%1+%2];" : "=r"(*reinterpret_cast<unsigned*>(&h)) : "r"(a), "n"(OFF));
+  return __half22float2(h);
+}
+
 // Gather of one voxel column (fixed X, Y; y-map without a Z term) from
 // detector rows `row0` and `row0 + WX`, adding into s[0..NZ).  x advances by
 // |a3| < 1 per voxel, so the fraction is stepped by one add and the tap
-// pointer by a predicated increment instead of a floor per voxel.  ASC walks
+// address by a predicated increment instead of a floor per voxel.  ASC walks
 // z upwards (a3 >= 0), else downwards, so that x never decreases.  Rounding
 // of the stepped fraction stays below 4e-6 px over 32 voxels; the caller
 // leaves one pixel of window slack for it.
@@ -76,7 +96,9 @@ __device__ __forceinline__ void bp_column(float (&s)[NZ], const PT* row0, int WX
   const float flx = floorf(x);
   float fx = x - flx;
   const float step = fabsf(a3);
-  const PT* p = row0 + (magic_int(flx) + lxm);
+  static_assert(sizeof(PT) == 4, "FP32 windows");
+  uint32_t p = smem_u32(row0) + 4u * (uint32_t)(magic_int(flx) + lxm);
+  const uint32_t dr = 4u * (uint32_t)WX;
 #pragma unroll
   for (int i = 0; i < NZ; ++i) {
     const int z = ASC ? i : NZ - 1 - i;
@@ -84,10 +106,10 @@ __device__ __forceinline__ void bp_column(float (&s)[NZ], const PT* row0, int WX
       fx += step;
       const bool adv = fx >= 1.f;
       fx = adv ? fx - 1.f : fx;
-      p += adv ? 1 : 0;
+      p += adv ? 4u : 0u;
     }
-    const float p00 = to_f(p[0]), p10 = to_f(p[1]);
-    const float p01 = to_f(p[WX]), p11 = to_f(p[WX + 1]);
+    const float p00 = lds_f32<0>(p), p10 = lds_f32<4>(p);
+    const float p01 = lds_f32<0>(p + dr), p11 = lds_f32<4>(p + dr);
     const float r0 = fmaf(fx, p10 - p00, p00);
     const float r1 = fmaf(fx, p11 - p01, p01);
     s[z] = fmaf(wy0, r0, s[z]);
@@ -104,7 +126,7 @@ __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float* b
   const float flx = floorf(x);
   float fx = x - flx;
   const float step = fabsf(a3);
-  const float* p = b + (magic_int(flx) + lxm);
+  uint32_t p = smem_u32(b) + 4u * (uint32_t)(magic_int(flx) + lxm);
 #pragma unroll
   for (int i = 0; i < NZ; ++i) {
     const int z = ASC ? i : NZ - 1 - i;
@@ -112,9 +134,9 @@ __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float* b
       fx += step;
       const bool adv = fx >= 1.f;
       fx = adv ? fx - 1.f : fx;
-      p += adv ? 1 : 0;
+      p += adv ? 4u : 0u;
     }
-    const float p0 = p[0], p1 = p[1];
+    const float p0 = lds_f32<0>(p), p1 = lds_f32<4>(p);
     s[z] += fmaf(fx, p1 - p0, p0);
   }
 }
@@ -130,7 +152,8 @@ __device__ __forceinline__ void bp_column(float (&s)[NZ], const float2* row0, in
   const float flx = floorf(x);
   float fx = x - flx;
   const float step = fabsf(a3);
-  const float2* p = row0 + (magic_int(flx) + lxm);
+  uint32_t p = smem_u32(row0) + 8u * (uint32_t)(magic_int(flx) + lxm);
+  const uint32_t dr = 8u * (uint32_t)WX;
 #pragma unroll
   for (int i = 0; i < NZ; ++i) {
     const int z = ASC ? i : NZ - 1 - i;
@@ -138,9 +161,9 @@ __device__ __forceinline__ void bp_column(float (&s)[NZ], const float2* row0, in
       fx += step;
       const bool adv = fx >= 1.f;
       fx = adv ? fx - 1.f : fx;
-      p += adv ? 1 : 0;
+      p += adv ? 8u : 0u;
     }
-    const float2 q0 = p[0], q1 = p[WX];
+    const float2 q0 = lds_f32x2<0>(p), q1 = lds_f32x2<0>(p + dr);
     s[z] = fmaf(wy0, fmaf(fx, q0.y, q0.x), s[z]);
     s[z] = fmaf(wy1, fmaf(fx, q1.y, q1.x), s[z]);
   }
@@ -157,8 +180,8 @@ __device__ __forceinline__ void bp_column_planar(float (&s)[NZ], const float* ro
   const float flx = floorf(x);
   float fx = x - flx;
   const float step = fabsf(a3);
-  const float* p = row0 + (magic_int(flx) + lxm);
-  const int w2 = 2 * WX, w3 = 3 * WX;
+  uint32_t p = smem_u32(row0) + 4u * (uint32_t)(magic_int(flx) + lxm);
+  const uint32_t d1 = 4u * (uint32_t)WX, d2 = 2u * d1, d3 = 3u * d1;
 #pragma unroll
   for (int i = 0; i < NZ; ++i) {
     const int z = ASC ? i : NZ - 1 - i;
@@ -166,10 +189,10 @@ __device__ __forceinline__ void bp_column_planar(float (&s)[NZ], const float* ro
       fx += step;
       const bool adv = fx >= 1.f;
       fx = adv ? fx - 1.f : fx;
-      p += adv ? 1 : 0;
+      p += adv ? 4u : 0u;
     }
-    s[z] = fmaf(wy0, fmaf(fx, p[WX], p[0]), s[z]);
-    s[z] = fmaf(wy1, fmaf(fx, p[w3], p[w2]), s[z]);
+    s[z] = fmaf(wy0, fmaf(fx, lds_f32<0>(p + d1), lds_f32<0>(p)), s[z]);
+    s[z] = fmaf(wy1, fmaf(fx, lds_f32<0>(p + d3), lds_f32<0>(p + d2)), s[z]);
   }
 }
 
@@ -184,7 +207,8 @@ __device__ __forceinline__ void bp_column_half(float (&s)[NZ], const __half2* ro
   const float flx = floorf(x);
   float fx = x - flx;
   const float step = fabsf(a3);
-  const __half2* p = row0 + (magic_int(flx) + lxm);
+  uint32_t p = smem_u32(row0) + 4u * (uint32_t)(magic_int(flx) + lxm);
+  const uint32_t dr = 4u * (uint32_t)WX;
 #pragma unroll
   for (int i = 0; i < NZ; ++i) {
     const int z = ASC ? i : NZ - 1 - i;
@@ -192,9 +216,9 @@ __device__ __forceinline__ void bp_column_half(float (&s)[NZ], const __half2* ro
       fx += step;
       const bool adv = fx >= 1.f;
       fx = adv ? fx - 1.f : fx;
-      p += adv ? 1 : 0;
+      p += adv ? 4u : 0u;
     }
-    const float2 q0 = __half22float2(p[0]), q1 = __half22float2(p[WX]);
+    const float2 q0 = lds_h2_widened<0>(p), q1 = lds_h2_widened<0>(p + dr);
     s[z] = fmaf(wy0, fmaf(fx, q0.y, q0.x), s[z]);
     s[z] = fmaf(wy1, fmaf(fx, q1.y, q1.x), s[z]);
   }
@@ -207,7 +231,7 @@ __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float2* 
   const float flx = floorf(x);
   float fx = x - flx;
   const float step = fabsf(a3);
-  const float2* p = b + (magic_int(flx) + lxm);
+  uint32_t p = smem_u32(b) + 8u * (uint32_t)(magic_int(flx) + lxm);
 #pragma unroll
   for (int i = 0; i < NZ; ++i) {
     const int z = ASC ? i : NZ - 1 - i;
@@ -215,9 +239,9 @@ __device__ __forceinline__ void bp_column_blended(float (&s)[NZ], const float2* 
       fx += step;
       const bool adv = fx >= 1.f;
       fx = adv ? fx - 1.f : fx;
-      p += adv ? 1 : 0;
+      p += adv ? 8u : 0u;
     }
-    const float2 q = p[0];
+    const float2 q = lds_f32x2<0>(p);
     s[z] += fmaf(fx, q.y, q.x);
   }
 }
