@@ -58,8 +58,8 @@ NCU_PROFILES = {
     ("c2", "backproject"): {"traffic": 390_982_656 + 167_104_768, "warp_inst": 828_349_812,
                             "duration_ms": 0.937248, "sm_ghz": 2.070, "sms": 152,
                             "source": "profiles/bp_tma_kernel_3axis_512x512x128.md"},
-    ("c2", "forward"): {"traffic": 128_372_224 + 37_204_480, "warp_inst": 1_447_238_792,
-                        "duration_ms": 1.489216, "sm_ghz": 2.066, "sms": 152,
+    ("c2", "forward"): {"traffic": 128_399_104 + 40_043_008, "warp_inst": 1_279_387_488,
+                        "duration_ms": 1.282304, "sm_ghz": 2.047, "sms": 152,
                         "source": "profiles/fwd_tma_kernel_3axis_512x512x128.md"},
 }
 
