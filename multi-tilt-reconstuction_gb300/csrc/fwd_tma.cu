@@ -330,8 +330,8 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
         const int q = urow[i];
         if (q != 0) {
           const float uf = (float)q;
-          atomicAdd(rowp + i, __float2int_rn((1.f - fy) * uf));
-          atomicAdd(rowp + WX + i, __float2int_rn(fy * uf));
+          red_shared(smem_u32(rowp + i), __float2int_rn((1.f - fy) * uf));
+          red_shared(smem_u32(rowp + WX + i), __float2int_rn(fy * uf));
           urow[i] = 0;
         }
       }
@@ -366,10 +366,11 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
         int* r0 = rowp + (magic_int(flx) + k.lxm);
         const float g0 = wy0 * v[z], g1 = wy1 * v[z];
         const float wx0 = 1.f - fx;
-        atomicAdd(r0, fixq(wx0, g0));
-        atomicAdd(r0 + 1, fixq(fx, g0));
-        atomicAdd(r0 + WX, fixq(wx0, g1));
-        atomicAdd(r0 + WX + 1, fixq(fx, g1));
+        const uint32_t a0 = smem_u32(r0), a1 = a0 + 4u * (uint32_t)WX;
+        red_shared(a0, fixq(wx0, g0));
+        red_shared(a0 + 4u, fixq(fx, g0));
+        red_shared(a1, fixq(wx0, g1));
+        red_shared(a1 + 4u, fixq(fx, g1));
       }
     } else if (active) {
       const float xr = fmaf(k.a2, (float)ty, fmaf(k.a1, (float)tx, k.xf));
@@ -408,12 +409,12 @@ __device__ __forceinline__ void fwd_brick(const CUtensorMap* smap, const FwdArgs
         const float wx0 = 1.f - fx;
         int* r0 = wi + (rowi * WX + ix);
         if (y0ok) {
-          if (x0ok) atomicAdd(r0, fixq(wx0, g0));
-          if (x1ok) atomicAdd(r0 + 1, fixq(fx, g0));
+          if (x0ok) red_shared(smem_u32(r0), fixq(wx0, g0));
+          if (x1ok) red_shared(smem_u32(r0 + 1), fixq(fx, g0));
         }
         if (y1ok) {
-          if (x0ok) atomicAdd(r0 + WX, fixq(wx0, g1));
-          if (x1ok) atomicAdd(r0 + WX + 1, fixq(fx, g1));
+          if (x0ok) red_shared(smem_u32(r0 + WX), fixq(wx0, g1));
+          if (x1ok) red_shared(smem_u32(r0 + WX + 1), fixq(fx, g1));
         }
       }
     }
