@@ -25,9 +25,12 @@
 // divided by S (exact: S is a power of two).
 //
 // When the y-map has no Z term, a voxel column's y weights are common to the
-// column and its x advances by |a3| < 1 per voxel: the interior path merges
+// column and its x advances by |a3| < 1 per voxel: the column walk merges
 // the column's 1-D splat in registers and adds one value per pixel it leaves
-// (2-16x fewer shared-memory adds than four per voxel, depending on the tilt).
+// (2-16x fewer shared-memory adds than four per voxel, depending on the tilt),
+// in branch-free chunks where the slope allows, with red.shared adds on 32-bit
+// shared addresses; bricks at the detector edge check each add against the
+// window.  The per-tap path remains for z-dependent y-maps and slopes >= 0.999.
 //
 // Windows are clamped inside the detector (TMA reduces must not start at a
 // negative coordinate), so a tap is on the detector iff it lies in the valid
