@@ -44,11 +44,14 @@ typedef enum mtr_status {
 /* Storage precision.  FP32: everything float.  MIXED_*: projections stored
  * FP16, the volume copy read by the forward projector stored BF16 (or FP16),
  * the per-axis MACE states w_k stored as FP16 deviations from the FP32
- * consensus (w_k - w_avg, rounded once per outer iteration); interpolation
- * and accumulation in FP32; residual norms and the
- * MACE consensus sum in FP64; the SIRT iterate (updated every iteration), the
- * residual, the weight sums and the consensus stay FP32.  Mixed storage takes
- * less device memory than FP32; values must lie within the FP16 range. */
+ * consensus (w_k - w_avg, rounded once per outer iteration), and, where the
+ * tuner finds it faster, the residual read by the back-projection stored as
+ * FP16 (value, next - value) pairs computed in FP32; interpolation and
+ * accumulation in FP32; residual norms and the MACE consensus sum in FP64;
+ * the SIRT iterate (updated every iteration), the weight sums and the
+ * consensus stay FP32.  Mixed storage takes less device memory than FP32;
+ * values (and residual differences) must lie within the FP16 range.
+ * MIXED_FP16 is the more accurate of the two (its copy keeps 11 bits). */
 typedef enum mtr_precision {
   MTR_PREC_FP32 = 0,
   MTR_PREC_MIXED_BF16 = 1,
